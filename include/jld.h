@@ -1,0 +1,215 @@
+/*
+ * jld.h — C ABI of the GB300 (sm_103a) Lagrangian-Deep-Learning hot path.
+ *
+ * These entry points replace the XLA CPU custom-call targets that the
+ * reference registers in lib/cpu.cc:271-292 (ppaint_*, preadout_*,
+ * ppaint3D_*, preadout3D_*, buildplan_*, pfft_*, pifft_*, initLayout,
+ * clean_*) for a world size of one.  Differences from the reference ABI:
+ *
+ *  - Every call is stream-ordered: it takes the cudaStream_t to launch on
+ *    and device pointers to caller-owned buffers.  Nothing is allocated on a
+ *    compute call; FFT twiddle tables are built once per (shape, dtype, device)
+ *    by jld_buildplan_* (or lazily by the first FFT call, which must then
+ *    happen outside stream capture).
+ *  - Every call returns an int status (JLD_OK or a JLD_ERR_* code) and sets
+ *    a thread-local message readable with jld_last_error().  The reference's
+ *    custom calls return void (lib/cpu.cc:52) and throw from inside
+ *    (lib/parops_fast.h:186).
+ *  - The readouts are stateless: they use the positions passed to them,
+ *    where the reference reads positions stored by the previous ppaint
+ *    (lib/cpu.cc:93,137; lib/parops_fast.h:534-561).
+ *  - The MPI communicator, layout index and edge arrays disappear: at world
+ *    size one the decomposition of lib/parops_fast.h:52-161 keeps every
+ *    particle on the local rank in input order, and the edges cover the whole
+ *    mesh.
+ *
+ * Positions "in mesh units" are what the reference's custom calls receive
+ * after jaxpops_bind.py:163-164 (pos % BoxSize, then / (BoxSize/Nmesh)),
+ * flattened row-major as (N, 3).  The *_box entry points take positions in
+ * box units and apply that same prelude on the device.
+ *
+ * Meshes are row-major (Nx, Ny, Nz), z fastest.  Half spectra are row-major
+ * (Nx, Ny, Nz/2+1) — split into real and imaginary planes for the
+ * reference-shaped pfft/pifft (lib/cpu.cc:169-245), interleaved complex for
+ * the *_c variants.  Nz must be even.
+ */
+#ifndef JLD_H_
+#define JLD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define JLD_API __attribute__((visibility("default")))
+#else
+#define JLD_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* jld_stream_t; /* == cudaStream_t */
+
+enum {
+  JLD_OK = 0,
+  JLD_ERR_ARG = 1,         /* null pointer, negative count, bad flag value */
+  JLD_ERR_UNSUPPORTED = 2, /* mesh size the FFT does not factor (2,3,5), odd Nz */
+  JLD_ERR_WORKSPACE = 3,   /* workspace pointer null or smaller than required */
+  JLD_ERR_CUDA = 4,        /* a CUDA runtime call failed; see jld_last_error() */
+  JLD_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  JLD_ERR_NOPLAN = 6       /* FFT plan missing while the stream is capturing */
+};
+
+/* Library identity and error reporting (no reference counterpart). */
+JLD_API const char* jld_version(void);
+JLD_API const char* jld_status_string(int status);
+JLD_API const char* jld_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Layout bookkeeping.                                                  */
+/* initLayout (lib/cpu.cc:29-38, lib/parops_fast.h:35-41) and clean_f32 / */
+/* clean_f64 (lib/cpu.cc:40-49, lib/parops_fast.h:43-48).  Stateless      */
+/* here: both validate lyidx (0..4, jaxpops_bind.py:157) and return.      */
+JLD_API int jld_init_layout(int32_t commsize, int32_t lyidx);
+JLD_API int jld_clean(int32_t lyidx);
+
+/* ------------------------------------------------------------------ */
+/* CIC paint.  ppaint_f32 / ppaint_f64: lib/cpu.cc:51-72 ->            */
+/* lib/parops_fast.h:484-531 (lpaint 354-411).  out is overwritten     */
+/* (zeroed, then painted).  mass has nparts entries.                   */
+JLD_API int jld_ppaint_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                   const float* mass, int32_t nx, int32_t ny, int32_t nz,
+                   float* out);
+JLD_API int jld_ppaint_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                   const double* mass, int64_t nx, int64_t ny, int64_t nz,
+                   double* out);
+
+/* Same paint on box-unit positions with the jaxpops_bind.py:161-164    */
+/* prelude fused (mass broadcast, pos % box, / (box/N)).  mass may be   */
+/* NULL, in which case every particle weighs mass_scalar.              */
+JLD_API int jld_ppaint_box_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                       const float* mass, float mass_scalar,
+                       int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                       float* out);
+JLD_API int jld_ppaint_box_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                       const double* mass, double mass_scalar,
+                       int64_t nx, int64_t ny, int64_t nz, const double box[3],
+                       double* out);
+
+/* Paint variants of the same box-unit paint (no reference counterpart;  */
+/* same contract and results within float rounding):                    */
+/*   method 0 = plain atomics, 1 = warp-aggregated atomics.             */
+JLD_API int jld_ppaint_box_method_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                              const float* mass, float mass_scalar,
+                              int32_t nx, int32_t ny, int32_t nz,
+                              const float box[3], int32_t method, float* out);
+
+/* Cell key of every particle: ((i % Nx) * Ny + j % Ny) * Nz + k % Nz with */
+/* i = int(p_x) etc., the per-particle key of the reference's             */
+/* decomposition (lib/parops_fast.h:91-93).  box == NULL: positions are in */
+/* mesh units; otherwise box units with the jaxpops_bind.py:163-164        */
+/* prelude applied.  keys has nparts int32 entries.                        */
+JLD_API int jld_cell_keys_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                      int32_t nx, int32_t ny, int32_t nz, const float* box,
+                      int32_t* keys);
+JLD_API int jld_cell_keys_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                      int64_t nx, int64_t ny, int64_t nz, const double* box,
+                      int32_t* keys);
+
+/* ------------------------------------------------------------------ */
+/* CIC readout.  preadout_f32 / preadout_f64: lib/cpu.cc:74-94 ->       */
+/* lib/parops_fast.h:533-567 (lreadout 414-481).  vjpdim = -1 reads the  */
+/* field; vjpdim = d in {0,1,2} replaces the weight along d by its       */
+/* derivative (+-Nmesh_d/box_d), as in lib/parops_fast.h:448-451.        */
+JLD_API int jld_preadout_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                     const float* field, int32_t nx, int32_t ny, int32_t nz,
+                     const float box[3], int32_t vjpdim, float* out);
+JLD_API int jld_preadout_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                     const double* field, int64_t nx, int64_t ny, int64_t nz,
+                     const double box[3], int32_t vjpdim, double* out);
+JLD_API int jld_preadout_box_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                         const float* field, int32_t nx, int32_t ny, int32_t nz,
+                         const float box[3], int32_t vjpdim, float* out);
+JLD_API int jld_preadout_box_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                         const double* field, int64_t nx, int64_t ny, int64_t nz,
+                         const double box[3], int32_t vjpdim, double* out);
+
+/* ------------------------------------------------------------------ */
+/* 3-channel paint.  ppaint3D_f32 / _f64: lib/cpu.cc:96-116 ->          */
+/* lib/parops_fast.h:678-725 (lpaint3D 615-676).  mass is (nparts, 3)    */
+/* row-major; out is (3, Nx, Ny, Nz).                                   */
+JLD_API int jld_ppaint3d_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                     const float* mass, int32_t nx, int32_t ny, int32_t nz,
+                     float* out);
+JLD_API int jld_ppaint3d_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                     const double* mass, int64_t nx, int64_t ny, int64_t nz,
+                     double* out);
+JLD_API int jld_ppaint3d_box_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                         const float* mass, int32_t nx, int32_t ny, int32_t nz,
+                         const float box[3], float* out);
+JLD_API int jld_ppaint3d_box_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                         const double* mass, int64_t nx, int64_t ny, int64_t nz,
+                         const double box[3], double* out);
+
+/* ------------------------------------------------------------------ */
+/* 3-channel readout.  preadout3D_f32 / _f64: lib/cpu.cc:118-138 ->      */
+/* lib/parops_fast.h:823-857 (lreadout3D 729-821).  vjp = 0: field is    */
+/* (3, Nx, Ny, Nz) and channel d is read into out[:, d]; vjp = 1: field  */
+/* is one mesh and out[:, d] is its CIC-weight gradient along d.          */
+JLD_API int jld_preadout3d_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                       const float* field, int32_t nx, int32_t ny, int32_t nz,
+                       const float box[3], int32_t vjp, float* out);
+JLD_API int jld_preadout3d_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                       const double* field, int64_t nx, int64_t ny, int64_t nz,
+                       const double box[3], int32_t vjp, double* out);
+JLD_API int jld_preadout3d_box_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                           const float* field, int32_t nx, int32_t ny, int32_t nz,
+                           const float box[3], int32_t vjp, float* out);
+JLD_API int jld_preadout3d_box_f64(jld_stream_t stream, const double* pos, int64_t nparts,
+                           const double* field, int64_t nx, int64_t ny, int64_t nz,
+                           const double box[3], int32_t vjp, double* out);
+
+/* ------------------------------------------------------------------ */
+/* FFT plans.  buildplan_f32 / _f64: lib/cpu.cc:140-167 ->               */
+/* lib/parfft.h:33-76.  Builds (once per device) the FP64-generated      */
+/* twiddle tables for this shape and returns {localL, localstart} =      */
+/* {Nx, 0}.  Call before any CUDA-graph capture that runs an FFT.        */
+JLD_API int jld_buildplan_f32(int32_t nx, int32_t ny, int32_t nz, int32_t local_out[2]);
+JLD_API int jld_buildplan_f64(int32_t nx, int32_t ny, int32_t nz, int32_t local_out[2]);
+
+/* Workspace bytes the FFT entry points need (Nx*Ny*(Nz/2+1) complex).  */
+JLD_API size_t jld_fft_workspace_f32(int32_t nx, int32_t ny, int32_t nz);
+JLD_API size_t jld_fft_workspace_f64(int32_t nx, int32_t ny, int32_t nz);
+
+/* pfft_f32 / pfft_f64: lib/cpu.cc:169-200 -> lib/parfft.h:78-94,111-125. */
+/* Unnormalised forward r2c DFT (sign -1); re/im are (Nx, Ny, Nz/2+1).    */
+JLD_API int jld_pfft_f32(jld_stream_t stream, const float* data, int32_t nx, int32_t ny,
+                 int32_t nz, float* re, float* im, void* ws, size_t ws_bytes);
+JLD_API int jld_pfft_f64(jld_stream_t stream, const double* data, int32_t nx, int32_t ny,
+                 int32_t nz, double* re, double* im, void* ws, size_t ws_bytes);
+/* Interleaved-complex output variant of the same transform.              */
+JLD_API int jld_pfft_c_f32(jld_stream_t stream, const float* data, int32_t nx, int32_t ny,
+                   int32_t nz, void* out_c, void* ws, size_t ws_bytes);
+JLD_API int jld_pfft_c_f64(jld_stream_t stream, const double* data, int32_t nx, int32_t ny,
+                   int32_t nz, void* out_c, void* ws, size_t ws_bytes);
+
+/* pifft_f32 / pifft_f64: lib/cpu.cc:202-245 -> lib/parfft.h:96-109,     */
+/* 127-138.  Unnormalised inverse c2r DFT (sign +1): complex inverse     */
+/* along x and y, then a c2r along z that ignores the imaginary parts of  */
+/* kz = 0 and kz = Nz/2.                                                  */
+JLD_API int jld_pifft_f32(jld_stream_t stream, const float* re, const float* im,
+                  int32_t nx, int32_t ny, int32_t nz, float* out,
+                  void* ws, size_t ws_bytes);
+JLD_API int jld_pifft_f64(jld_stream_t stream, const double* re, const double* im,
+                  int32_t nx, int32_t ny, int32_t nz, double* out,
+                  void* ws, size_t ws_bytes);
+JLD_API int jld_pifft_c_f32(jld_stream_t stream, const void* in_c, int32_t nx, int32_t ny,
+                    int32_t nz, float* out, void* ws, size_t ws_bytes);
+JLD_API int jld_pifft_c_f64(jld_stream_t stream, const void* in_c, int32_t nx, int32_t ny,
+                    int32_t nz, double* out, void* ws, size_t ws_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JLD_H_ */

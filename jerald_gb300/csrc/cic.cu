@@ -1,0 +1,502 @@
+// Cloud-in-cell paint and readout on sm_103a.
+//
+// Device restatement of the single-rank CIC loops of the reference:
+//   lpaint     lib/parops_fast.h:354-411    -> paint_kernel
+//   lreadout   lib/parops_fast.h:414-481    -> readout_kernel
+//   lpaint3D   lib/parops_fast.h:616-676    -> paint3_kernel
+//   lreadout3D lib/parops_fast.h:730-821    -> readout3_kernel
+// At world size one the decomposition/exchange/gather steps
+// (lib/parops_fast.h:52-351) keep every particle local and in input order,
+// so each kernel walks the caller's particle array directly.
+//
+// Paint scatters with global float/double atomics (red.global.add), one per
+// corner.  The warp-aggregated variant first merges lanes of a warp that hit
+// the same cell (__match_any_sync) so clustered inputs issue fewer atomics.
+// Readouts gather the eight corners; weights and sums use explicit
+// round-to-nearest intrinsics so they follow the reference's operation order.
+
+#include "common.cuh"
+
+namespace jld {
+
+template <typename T>
+struct PosSrc {
+  const T* pos;   // (N, 3) row-major
+  T box[3];       // used when BOX
+  T cell[3];      // box / N per axis, in T
+};
+
+template <typename T, bool BOX>
+__device__ __forceinline__ void load_pos(const PosSrc<T>& s, int64_t p, T q[3]) {
+  const T* src = s.pos + 3 * p;
+  T x = __ldg(src), y = __ldg(src + 1), z = __ldg(src + 2);
+  if (BOX) {
+    q[0] = box_to_mesh(x, s.box[0], s.cell[0]);
+    q[1] = box_to_mesh(y, s.box[1], s.cell[1]);
+    q[2] = box_to_mesh(z, s.box[2], s.cell[2]);
+  } else {
+    q[0] = x; q[1] = y; q[2] = z;
+  }
+}
+
+// Per-axis weights of corner `bits`: lower corner t = 1 - d, upper corner d.
+template <typename T>
+__device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bits) {
+  T wx = (bits & 1) ? hi[0] : lo[0];
+  T wy = (bits & 2) ? hi[1] : lo[1];
+  T wz = (bits & 4) ? hi[2] : lo[2];
+  return mul_rn(mul_rn(wx, wy), wz);
+}
+
+// ---------------------------------------------------------------------------
+// Paint (single channel).  mass == nullptr => every particle weighs mscalar.
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
+             Grid3 g, T* __restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    T q[3];
+    load_pos<T, BOX>(src, p, q);
+    Corners<T> c;
+    cic_corners(q, g, c);
+    T lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+    T m = mass ? __ldg(mass + p) : mscalar;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      int bits = corner_axis_bits(k);
+      T w = mul_rn(corner_weight(lo, hi, bits), m);
+      w = mul_rn(w, corner_ok(c, bits) ? T(1) : T(0));
+      atomicAdd(out + corner_offset(c, bits, g), w);
+    }
+  }
+}
+
+// Warp-aggregated paint: lanes of a warp whose corner falls in the same cell
+// add their weights (in ascending lane order) and one leader lane issues the
+// atomic.  Every lane of the warp runs the loop body so the warp-wide
+// intrinsics see a full mask; out-of-range lanes carry weight 0 at cell -1.
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+paint_warpagg_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass,
+                     T mscalar, Grid3 g, T* __restrict__ out) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t base0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
+  for (int64_t base = base0; base < n; base += stride) {
+    int64_t p = base + lane;
+    bool live = p < n;
+    T q[3] = {T(0), T(0), T(0)};
+    T m = T(0);
+    if (live) {
+      load_pos<T, BOX>(src, p, q);
+      m = mass ? __ldg(mass + p) : mscalar;
+    }
+    Corners<T> c;
+    cic_corners(q, g, c);
+    T lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+      int bits = corner_axis_bits(k);
+      T w = mul_rn(corner_weight(lo, hi, bits), m);
+      w = mul_rn(w, corner_ok(c, bits) ? T(1) : T(0));
+      long long cell = live ? (long long)corner_offset(c, bits, g) : -1ll;
+      unsigned peers = __match_any_sync(full, cell);
+      int leader = __ffs(peers) - 1;
+      T sum = T(0);
+      unsigned rem = peers;
+      while (__any_sync(full, rem != 0u)) {
+        int srcl = rem ? (__ffs(rem) - 1) : lane;
+        T t = __shfl_sync(full, w, srcl);
+        if (rem) { sum = sum + t; rem &= rem - 1u; }
+      }
+      if (lane == leader && cell >= 0) atomicAdd(out + cell, sum);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Three-channel paint: mass (N,3) row-major, out (3, C).
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+paint3_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, Grid3 g,
+              T* __restrict__ out) {
+  const int64_t C = g.cells();
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    T q[3];
+    load_pos<T, BOX>(src, p, q);
+    Corners<T> c;
+    cic_corners(q, g, c);
+    T lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+    T m3[3] = {__ldg(mass + 3 * p), __ldg(mass + 3 * p + 1), __ldg(mass + 3 * p + 2)};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        int bits = corner_axis_bits(k);
+        T w = mul_rn(corner_weight(lo, hi, bits), m3[d]);
+        w = mul_rn(w, corner_ok(c, bits) ? T(1) : T(0));
+        atomicAdd(out + d * C + corner_offset(c, bits, g), w);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Readout of one field; vjpdim in {-1, 0, 1, 2}.
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+readout_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ field, Grid3 g,
+               int vjpdim, T dweight, T* __restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    T q[3];
+    load_pos<T, BOX>(src, p, q);
+    Corners<T> c;
+    cic_corners(q, g, c);
+    T lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+    if (vjpdim >= 0) { hi[vjpdim] = dweight; lo[vjpdim] = -dweight; }
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      int bits = corner_axis_bits(k);
+      T v = __ldg(field + corner_offset(c, bits, g));
+      T t = mul_rn(mul_rn(corner_weight(lo, hi, bits), v),
+                   corner_ok(c, bits) ? T(1) : T(0));
+      acc = (k == 0) ? t : add_rn(acc, t);
+    }
+    out[p] = acc;
+  }
+}
+
+// Three-channel readout.  vjp == 0: out[p,d] reads channel d of a (3, C)
+// field.  vjp == 1: out[p,d] is the weight gradient along d of one field.
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+readout3_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ field, Grid3 g,
+                int vjp, T dw0, T dw1, T dw2, T* __restrict__ out) {
+  const int64_t C = g.cells();
+  const T dw[3] = {dw0, dw1, dw2};
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    T q[3];
+    load_pos<T, BOX>(src, p, q);
+    Corners<T> c;
+    cic_corners(q, g, c);
+    T lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      T lo_d[3] = {lo[0], lo[1], lo[2]};
+      T hi_d[3] = {hi[0], hi[1], hi[2]};
+      const T* f = field;
+      if (vjp) { hi_d[d] = dw[d]; lo_d[d] = -dw[d]; }
+      else f = field + d * C;
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        int bits = corner_axis_bits(k);
+        T v = __ldg(f + corner_offset(c, bits, g));
+        T t = mul_rn(mul_rn(corner_weight(lo_d, hi_d, bits), v),
+                     corner_ok(c, bits) ? T(1) : T(0));
+        acc = (k == 0) ? t : add_rn(acc, t);
+      }
+      out[3 * p + d] = acc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cell keys: flattened index of int(p) % N per axis, the key the reference's
+// decomposition computes for each particle (lib/parops_fast.h:91-93).
+template <typename T, bool BOX>
+__global__ void __launch_bounds__(256)
+keys_kernel(PosSrc<T> src, int64_t n, Grid3 g, int32_t* __restrict__ keys) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    T q[3];
+    load_pos<T, BOX>(src, p, q);
+    int i = (int)q[0] % g.nx, j = (int)q[1] % g.ny, k = (int)q[2] % g.nz;
+    keys[p] = (int32_t)(((int64_t)i * g.ny + j) * g.nz + k);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+template <typename T>
+static int check_common(const void* pos, int64_t nparts, const void* out,
+                        int64_t nx, int64_t ny, int64_t nz, const char* who) {
+  if (nparts < 0) return set_error(JLD_ERR_ARG, "%s: nparts < 0", who);
+  if (nparts > 0 && !pos) return set_error(JLD_ERR_ARG, "%s: pos is NULL", who);
+  if (!out) return set_error(JLD_ERR_ARG, "%s: output is NULL", who);
+  if (nx <= 0 || ny <= 0 || nz <= 0)
+    return set_error(JLD_ERR_ARG, "%s: mesh sizes must be positive", who);
+  if (nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30))
+    return set_error(JLD_ERR_ARG, "%s: mesh size too large", who);
+  return JLD_OK;
+}
+
+template <typename T>
+static PosSrc<T> make_src(const T* pos, const T* box, int64_t nx, int64_t ny,
+                          int64_t nz) {
+  PosSrc<T> s;
+  s.pos = pos;
+  const int64_t n[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a) {
+    s.box[a] = box ? box[a] : T(1);
+    s.cell[a] = box ? (T)(box[a] / (T)n[a]) : T(1);
+  }
+  return s;
+}
+
+template <typename T>
+static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* mass,
+                      T mscalar, int64_t nx, int64_t ny, int64_t nz, const T* box,
+                      int method, T* out, const char* who) {
+  int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
+  if (s) return s;
+  if (box && !(box[0] > 0 && box[1] > 0 && box[2] > 0))
+    return set_error(JLD_ERR_ARG, "%s: box sizes must be positive", who);
+  Grid3 g = make_grid(nx, ny, nz);
+  JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(T) * g.cells(), st));
+  if (nparts == 0) return JLD_OK;
+  PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  const int block = 256;
+  unsigned grid = grid_for(nparts, block);
+  if (method == 1) {
+    if (box) paint_warpagg_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+    else paint_warpagg_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+  } else {
+    if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+    else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+  }
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
+template <typename T>
+static int paint3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* mass,
+                       int64_t nx, int64_t ny, int64_t nz, const T* box, T* out,
+                       const char* who) {
+  int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
+  if (s) return s;
+  if (nparts > 0 && !mass) return set_error(JLD_ERR_ARG, "%s: mass is NULL", who);
+  Grid3 g = make_grid(nx, ny, nz);
+  JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(T) * 3 * g.cells(), st));
+  if (nparts == 0) return JLD_OK;
+  PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  const int block = 256;
+  unsigned grid = grid_for(nparts, block);
+  if (box) paint3_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, g, out);
+  else paint3_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, g, out);
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
+template <typename T>
+static int readout_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* field,
+                        int64_t nx, int64_t ny, int64_t nz, const T* box, bool boxpos,
+                        int vjpdim, T* out, const char* who) {
+  int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
+  if (s) return s;
+  if (!field) return set_error(JLD_ERR_ARG, "%s: field is NULL", who);
+  if (vjpdim < -1 || vjpdim > 2)
+    return set_error(JLD_ERR_ARG, "%s: vjpdim must be between -1 and 2", who);
+  if (vjpdim >= 0 && !box) return set_error(JLD_ERR_ARG, "%s: vjp needs box", who);
+  if (nparts == 0) return JLD_OK;
+  Grid3 g = make_grid(nx, ny, nz);
+  PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  const int64_t nm[3] = {nx, ny, nz};
+  T dweight = vjpdim >= 0 ? (T)((T)nm[vjpdim] / box[vjpdim]) : T(0);
+  const int block = 256;
+  unsigned grid = grid_for(nparts, block);
+  if (boxpos) readout_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
+  else readout_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
+template <typename T>
+static int readout3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* field,
+                         int64_t nx, int64_t ny, int64_t nz, const T* box, bool boxpos,
+                         int vjp, T* out, const char* who) {
+  int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
+  if (s) return s;
+  if (!field) return set_error(JLD_ERR_ARG, "%s: field is NULL", who);
+  if (vjp != 0 && vjp != 1) return set_error(JLD_ERR_ARG, "%s: vjp must be 0 or 1", who);
+  if (!box) return set_error(JLD_ERR_ARG, "%s: box is NULL", who);
+  if (nparts == 0) return JLD_OK;
+  Grid3 g = make_grid(nx, ny, nz);
+  PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  T dw[3];
+  const int64_t nm[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a) dw[a] = (T)((T)nm[a] / box[a]);
+  const int block = 256;
+  unsigned grid = grid_for(nparts, block);
+  if (boxpos) readout3_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
+  else readout3_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
+template <typename T>
+static int keys_impl(cudaStream_t st, const T* pos, int64_t nparts, int64_t nx, int64_t ny,
+                     int64_t nz, const T* box, int32_t* keys, const char* who) {
+  int s = check_common<T>(pos, nparts, keys, nx, ny, nz, who);
+  if (s) return s;
+  if (nx * ny * nz > INT32_MAX) return set_error(JLD_ERR_UNSUPPORTED, "%s: mesh too large for int32 keys", who);
+  if (nparts == 0) return JLD_OK;
+  Grid3 g = make_grid(nx, ny, nz);
+  PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  const int block = 256;
+  unsigned grid = grid_for(nparts, block);
+  if (box) keys_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, g, keys);
+  else keys_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, g, keys);
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
+}  // namespace jld
+
+using namespace jld;
+
+#define ST(s) reinterpret_cast<cudaStream_t>(s)
+
+extern "C" {
+
+int jld_ppaint_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass,
+                   int32_t nx, int32_t ny, int32_t nz, float* out) {
+  clear_error();
+  if (n > 0 && !mass) return set_error(JLD_ERR_ARG, "jld_ppaint_f32: mass is NULL");
+  return paint_impl<float>(ST(s), pos, n, mass, 0.f, nx, ny, nz, nullptr, 0, out, "jld_ppaint_f32");
+}
+int jld_ppaint_f64(jld_stream_t s, const double* pos, int64_t n, const double* mass,
+                   int64_t nx, int64_t ny, int64_t nz, double* out) {
+  clear_error();
+  if (n > 0 && !mass) return set_error(JLD_ERR_ARG, "jld_ppaint_f64: mass is NULL");
+  return paint_impl<double>(ST(s), pos, n, mass, 0.0, nx, ny, nz, nullptr, 0, out, "jld_ppaint_f64");
+}
+int jld_ppaint_box_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass,
+                       float ms, int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                       float* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint_box_f32: box is NULL");
+  return paint_impl<float>(ST(s), pos, n, mass, ms, nx, ny, nz, box, 0, out, "jld_ppaint_box_f32");
+}
+int jld_ppaint_box_f64(jld_stream_t s, const double* pos, int64_t n, const double* mass,
+                       double ms, int64_t nx, int64_t ny, int64_t nz, const double box[3],
+                       double* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint_box_f64: box is NULL");
+  return paint_impl<double>(ST(s), pos, n, mass, ms, nx, ny, nz, box, 0, out, "jld_ppaint_box_f64");
+}
+int jld_ppaint_box_method_f32(jld_stream_t s, const float* pos, int64_t n,
+                              const float* mass, float ms, int32_t nx, int32_t ny,
+                              int32_t nz, const float box[3], int32_t method, float* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint_box_method_f32: box is NULL");
+  if (method != 0 && method != 1)
+    return set_error(JLD_ERR_ARG, "jld_ppaint_box_method_f32: method must be 0 or 1");
+  return paint_impl<float>(ST(s), pos, n, mass, ms, nx, ny, nz, box, method, out,
+                           "jld_ppaint_box_method_f32");
+}
+
+int jld_preadout_f32(jld_stream_t s, const float* pos, int64_t n, const float* field,
+                     int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                     int32_t vjpdim, float* out) {
+  clear_error();
+  return readout_impl<float>(ST(s), pos, n, field, nx, ny, nz, box, false, vjpdim, out, "jld_preadout_f32");
+}
+int jld_preadout_f64(jld_stream_t s, const double* pos, int64_t n, const double* field,
+                     int64_t nx, int64_t ny, int64_t nz, const double box[3],
+                     int32_t vjpdim, double* out) {
+  clear_error();
+  return readout_impl<double>(ST(s), pos, n, field, nx, ny, nz, box, false, vjpdim, out, "jld_preadout_f64");
+}
+int jld_preadout_box_f32(jld_stream_t s, const float* pos, int64_t n, const float* field,
+                         int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                         int32_t vjpdim, float* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_preadout_box_f32: box is NULL");
+  return readout_impl<float>(ST(s), pos, n, field, nx, ny, nz, box, true, vjpdim, out, "jld_preadout_box_f32");
+}
+int jld_preadout_box_f64(jld_stream_t s, const double* pos, int64_t n, const double* field,
+                         int64_t nx, int64_t ny, int64_t nz, const double box[3],
+                         int32_t vjpdim, double* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_preadout_box_f64: box is NULL");
+  return readout_impl<double>(ST(s), pos, n, field, nx, ny, nz, box, true, vjpdim, out, "jld_preadout_box_f64");
+}
+
+int jld_ppaint3d_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass,
+                     int32_t nx, int32_t ny, int32_t nz, float* out) {
+  clear_error();
+  return paint3_impl<float>(ST(s), pos, n, mass, nx, ny, nz, nullptr, out, "jld_ppaint3d_f32");
+}
+int jld_ppaint3d_f64(jld_stream_t s, const double* pos, int64_t n, const double* mass,
+                     int64_t nx, int64_t ny, int64_t nz, double* out) {
+  clear_error();
+  return paint3_impl<double>(ST(s), pos, n, mass, nx, ny, nz, nullptr, out, "jld_ppaint3d_f64");
+}
+int jld_ppaint3d_box_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass,
+                         int32_t nx, int32_t ny, int32_t nz, const float box[3], float* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint3d_box_f32: box is NULL");
+  return paint3_impl<float>(ST(s), pos, n, mass, nx, ny, nz, box, out, "jld_ppaint3d_box_f32");
+}
+int jld_ppaint3d_box_f64(jld_stream_t s, const double* pos, int64_t n, const double* mass,
+                         int64_t nx, int64_t ny, int64_t nz, const double box[3], double* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint3d_box_f64: box is NULL");
+  return paint3_impl<double>(ST(s), pos, n, mass, nx, ny, nz, box, out, "jld_ppaint3d_box_f64");
+}
+
+int jld_preadout3d_f32(jld_stream_t s, const float* pos, int64_t n, const float* field,
+                       int32_t nx, int32_t ny, int32_t nz, const float box[3], int32_t vjp,
+                       float* out) {
+  clear_error();
+  return readout3_impl<float>(ST(s), pos, n, field, nx, ny, nz, box, false, vjp, out, "jld_preadout3d_f32");
+}
+int jld_preadout3d_f64(jld_stream_t s, const double* pos, int64_t n, const double* field,
+                       int64_t nx, int64_t ny, int64_t nz, const double box[3], int32_t vjp,
+                       double* out) {
+  clear_error();
+  return readout3_impl<double>(ST(s), pos, n, field, nx, ny, nz, box, false, vjp, out, "jld_preadout3d_f64");
+}
+int jld_preadout3d_box_f32(jld_stream_t s, const float* pos, int64_t n, const float* field,
+                           int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                           int32_t vjp, float* out) {
+  clear_error();
+  return readout3_impl<float>(ST(s), pos, n, field, nx, ny, nz, box, true, vjp, out, "jld_preadout3d_box_f32");
+}
+int jld_preadout3d_box_f64(jld_stream_t s, const double* pos, int64_t n, const double* field,
+                           int64_t nx, int64_t ny, int64_t nz, const double box[3],
+                           int32_t vjp, double* out) {
+  clear_error();
+  return readout3_impl<double>(ST(s), pos, n, field, nx, ny, nz, box, true, vjp, out, "jld_preadout3d_box_f64");
+}
+
+int jld_cell_keys_f32(jld_stream_t s, const float* pos, int64_t n, int32_t nx, int32_t ny,
+                      int32_t nz, const float* box, int32_t* keys) {
+  clear_error();
+  return keys_impl<float>(ST(s), pos, n, nx, ny, nz, box, keys, "jld_cell_keys_f32");
+}
+int jld_cell_keys_f64(jld_stream_t s, const double* pos, int64_t n, int64_t nx, int64_t ny,
+                      int64_t nz, const double* box, int32_t* keys) {
+  clear_error();
+  return keys_impl<double>(ST(s), pos, n, nx, ny, nz, box, keys, "jld_cell_keys_f64");
+}
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// Status strings, the thread-local error message and the stateless layout
+// entry points (initLayout / clean of lib/cpu.cc:29-49).
+
+#include "common.cuh"
+
+#include <string.h>
+
+namespace jld {
+
+static thread_local char g_msg[512] = "";
+
+int set_error(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+void clear_error() { g_msg[0] = '\0'; }
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    n = 148;
+  if (dev >= 0 && dev < 64) cached[dev] = n;
+  return n;
+}
+
+}  // namespace jld
+
+extern "C" {
+
+const char* jld_version(void) { return "jerald-gb300 0.1 (sm_103a)"; }
+
+const char* jld_status_string(int status) {
+  switch (status) {
+    case JLD_OK: return "ok";
+    case JLD_ERR_ARG: return "invalid argument";
+    case JLD_ERR_UNSUPPORTED: return "unsupported size";
+    case JLD_ERR_WORKSPACE: return "workspace too small";
+    case JLD_ERR_CUDA: return "CUDA error";
+    case JLD_ERR_TIMEOUT: return "device wait timed out";
+    case JLD_ERR_NOPLAN: return "FFT plan missing during stream capture";
+    default: return "unknown status";
+  }
+}
+
+const char* jld_last_error(void) { return jld::g_msg; }
+
+// The reference keeps up to five decomposition layouts indexed by lyidx
+// (lib/cpu.cc:15, jaxpops_bind.py:157).  This library keeps none; the entry
+// points only validate their arguments so callers get the same errors.
+int jld_init_layout(int32_t commsize, int32_t lyidx) {
+  jld::clear_error();
+  if (commsize != 1)
+    return jld::set_error(JLD_ERR_UNSUPPORTED, "initLayout: world size %d (only 1 is supported)",
+                          commsize);
+  if (lyidx < 0 || lyidx > 4)
+    return jld::set_error(JLD_ERR_ARG, "initLayout: lyidx needs to be between 0 and 4");
+  return JLD_OK;
+}
+
+int jld_clean(int32_t lyidx) {
+  jld::clear_error();
+  if (lyidx < 0 || lyidx > 4)
+    return jld::set_error(JLD_ERR_ARG, "clean: lyidx needs to be between 0 and 4");
+  return JLD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+// Shared helpers for the sm_103a kernels: status/error plumbing, the
+// mesh-coordinate prelude and the cloud-in-cell (CIC) corner arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdarg.h>
+
+#include "../../include/jld.h"
+
+namespace jld {
+
+// ---------------------------------------------------------------------------
+// Error reporting.  Every C entry point returns a status and leaves a
+// human-readable message in a thread-local buffer.
+int set_error(int status, const char* fmt, ...);
+void clear_error();
+
+#define JLD_CUDA_TRY(expr)                                                      \
+  do {                                                                          \
+    cudaError_t _e = (expr);                                                    \
+    if (_e != cudaSuccess)                                                      \
+      return ::jld::set_error(JLD_ERR_CUDA, "%s failed: %s (%s:%d)", #expr,     \
+                              cudaGetErrorString(_e), __FILE__, __LINE__);      \
+  } while (0)
+
+// Checks the launch that was just issued on the current thread.
+#define JLD_LAUNCH_CHECK(name)                                                  \
+  do {                                                                          \
+    cudaError_t _e = cudaGetLastError();                                        \
+    if (_e != cudaSuccess)                                                      \
+      return ::jld::set_error(JLD_ERR_CUDA, "launch of %s failed: %s", name,    \
+                              cudaGetErrorString(_e));                          \
+  } while (0)
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Grid size for a grid-stride loop over n items with the given block size:
+// enough CTAs to fill every SM `per_sm` times, never more than needed.
+inline unsigned grid_for(int64_t n, int block, int per_sm = 8) {
+  int64_t need = (n + block - 1) / block;
+  int64_t cap = (int64_t)sm_count() * per_sm;
+  if (need < 1) need = 1;
+  return (unsigned)(need < cap ? need : cap);
+}
+
+// ---------------------------------------------------------------------------
+// Mesh geometry passed by value to kernels.
+struct Grid3 {
+  int nx, ny, nz;      // mesh cells per axis
+  int64_t sy, sx;      // strides of y and x in a (nx, ny, nz) row-major mesh
+  __host__ __device__ int64_t cells() const { return sx * (int64_t)nx; }
+};
+
+inline Grid3 make_grid(int64_t nx, int64_t ny, int64_t nz) {
+  Grid3 g;
+  g.nx = (int)nx; g.ny = (int)ny; g.nz = (int)nz;
+  g.sy = nz;
+  g.sx = (int64_t)ny * nz;
+  return g;
+}
+
+// Box-to-mesh prelude of jaxpops_bind.py:163-164 in the working dtype:
+// r = x mod L with jnp.remainder semantics (C fmod, plus L when the signs of
+// r and L differ and r is nonzero), then r / (L/N) with IEEE division.
+template <typename T>
+__device__ __forceinline__ T box_to_mesh(T x, T box, T cell) {
+  T r = fmod(x, box);
+  if (r != T(0) && ((r < T(0)) != (box < T(0)))) r = r + box;
+  return r / cell;
+}
+
+// IEEE round-to-nearest products/sums without FMA contraction, so that the
+// CIC weights and readout sums follow the reference's operation order
+// (lib/parops_fast.h:376-409, 442-478) bit for bit.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// The eight CIC corners of one particle, in the order the reference visits
+// them (lib/parops_fast.h:402-409): (i,j,k) (i+1,j,k) (i,j+1,k) (i,j,k+1)
+// (i+1,j+1,k) (i+1,j,k+1) (i,j+1,k+1) (i+1,j+1,k+1).
+// `lo[a]` / `hi[a]` are the per-axis weights of the lower / upper corner
+// (t = 1-d and d in the reference), `ok_lo[a]` / `ok_hi[a]` the validity
+// flags (inx.. / inpx..) and `cell_lo[a]` / `cell_hi[a]` the wrapped
+// indices.  At world size one the rank edges are [0, N) on every axis.
+template <typename T>
+struct Corners {
+  int c_lo[3], c_hi[3];
+  bool ok_lo[3], ok_hi[3];
+  T d[3];  // fractional offsets p - int(p)
+};
+
+template <typename T>
+__device__ __forceinline__ void cic_corners(const T p[3], const Grid3& g,
+                                            Corners<T>& c) {
+  const int n[3] = {g.nx, g.ny, g.nz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int i = (int)p[a];                 // C++ int(): truncation toward zero
+    c.d[a] = sub_rn(p[a], (T)i);
+    int ip1 = (i + 1) % n[a];          // C remainder semantics
+    c.ok_lo[a] = (unsigned)i < (unsigned)n[a];
+    c.ok_hi[a] = (unsigned)ip1 < (unsigned)n[a];
+    c.c_lo[a] = abs(i % n[a]);
+    c.c_hi[a] = abs(ip1 % n[a]);
+  }
+}
+
+// Flattened cell offset of corner q (0..7, reference order).
+__device__ __forceinline__ int corner_axis_bits(int q) {
+  // bit a set => upper corner along axis a
+  // order: 000 100 010 001 110 101 011 111 (x is bit 0)
+  const int tab = (0) | (1 << 3) | (2 << 6) | (4 << 9) | (3 << 12) | (5 << 15) |
+                  (6 << 18) | (7 << 21);
+  return (tab >> (3 * q)) & 7;
+}
+
+template <typename T>
+__device__ __forceinline__ int64_t corner_offset(const Corners<T>& c, int bits,
+                                                 const Grid3& g) {
+  int ix = (bits & 1) ? c.c_hi[0] : c.c_lo[0];
+  int iy = (bits & 2) ? c.c_hi[1] : c.c_lo[1];
+  int iz = (bits & 4) ? c.c_hi[2] : c.c_lo[2];
+  return (int64_t)ix * g.sx + (int64_t)iy * g.sy + iz;
+}
+
+template <typename T>
+__device__ __forceinline__ bool corner_ok(const Corners<T>& c, int bits) {
+  return ((bits & 1) ? c.ok_hi[0] : c.ok_lo[0]) &&
+         ((bits & 2) ? c.ok_hi[1] : c.ok_lo[1]) &&
+         ((bits & 4) ? c.ok_hi[2] : c.ok_lo[2]);
+}
+
+}  // namespace jld

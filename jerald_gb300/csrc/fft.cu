@@ -1,0 +1,313 @@
+// 3-D real FFT pair on sm_103a: pencil passes over a split-Nyquist internal
+// half-spectrum, each pass a shared-memory Stockham transform (fft_core.cuh).
+//
+// Replaces the FFTW-MPI slab transforms of the reference:
+//   buildplan/buildplanf  lib/parfft.h:33-76   -> get_plan3 / jld_buildplan_*
+//   pfft/pfftf + split    lib/parfft.h:78-94,111-125, lib/cpu.cc:169-200
+//   pifft/pifftf + depad  lib/parfft.h:96-109,127-138, lib/cpu.cc:202-245
+// Conventions (FFTW's): forward r2c is unnormalised with sign -1 over all
+// three axes, keeping kz in [0, nz/2]; the inverse c2r is unnormalised with
+// sign +1, done as complex inverses along x and y followed by a c2r along z
+// that ignores the imaginary parts of kz = 0 and kz = nz/2.
+//
+// Forward (r2c):  z pass  real rows -> internal (even/odd packing: a length
+//                 nz real row is one length nz/2 complex FFT plus a split)
+//                 y pass  in place on the internal layout
+//                 x pass  internal -> caller layout (nx, ny, nz/2+1)
+// Inverse (c2r):  x pass  caller layout -> internal, y pass in place,
+//                 z pass  internal -> real rows.
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+#include <cmath>
+
+#include "fft_core.cuh"
+#include "fft_passes.cuh"
+
+namespace jld {
+
+// ---------------------------------------------------------------------------
+// Schedules.
+
+static int lcm_int(int a, int b) {
+  int x = a, y = b;
+  while (y) { int t = x % y; x = y; y = t; }
+  return a / x * b;
+}
+
+// Picks the radix sequence and elements-per-thread E for length n.
+// Powers of two use radix 16 (then 8/4/2), E = min(16, n).  Mixed lengths
+// use radices 4/2, 3 and 5 with E = lcm of the radices (at most 30).
+static bool make_line_schedule(int n, int* E, int* nst, int* radix) {
+  if (n < 1) return false;
+  int a = 0, b = 0, c = 0, m = n;
+  while (m % 2 == 0) { m /= 2; ++a; }
+  while (m % 3 == 0) { m /= 3; ++b; }
+  while (m % 5 == 0) { m /= 5; ++c; }
+  if (m != 1) return false;
+  int k = 0;
+  if (b == 0 && c == 0) {
+    while (a >= 4) { radix[k++] = 16; a -= 4; }
+    if (a == 3) radix[k++] = 8;
+    else if (a == 2) radix[k++] = 4;
+    else if (a == 1) radix[k++] = 2;
+  } else {
+    if (c == 0) {
+      while (a >= 2) { radix[k++] = 4; a -= 2; }
+      if (a == 1) radix[k++] = 2;
+    } else {
+      while (a >= 1) { radix[k++] = 2; a -= 1; }
+    }
+    while (b-- > 0) radix[k++] = 3;
+    while (c-- > 0) radix[k++] = 5;
+  }
+  if (k > kMaxStages) return false;
+  int e = 1;
+  for (int s = 0; s < k; ++s) e = lcm_int(e, radix[s]);
+  *E = e;
+  *nst = k;
+  return true;
+}
+
+int tile_cols(int n, int E, size_t elem_bytes) {
+  int cols = 16;
+  while (cols > 1 && (int64_t)cols * n / E > 512) cols >>= 1;
+  while (cols > 1 && (size_t)n * (cols + 1) * elem_bytes > 200 * 1024) cols >>= 1;
+  // Small transforms: widen the tile so a CTA has a useful number of threads.
+  while (cols < 64 && (int64_t)(cols * 2) * n / E <= 256 &&
+         (size_t)n * (cols * 2 + 1) * elem_bytes <= 48 * 1024)
+    cols <<= 1;
+  return cols;
+}
+
+// ---------------------------------------------------------------------------
+// Plan cache: one entry per (device, dtype, nx, ny, nz), never freed.
+
+struct PlanEntry {
+  int E[3], nst[3], radix[3][kMaxStages];
+  void* dev = nullptr;  // twiddle tables
+  size_t off[4];        // element offsets of tables x, y, z, r2c split
+};
+
+static std::mutex g_plan_mu;
+static std::map<std::tuple<int, int, int, int, int>, PlanEntry> g_plans;
+
+template <typename T>
+static void fill_twiddles(std::vector<cplx_t<T>>& v, size_t off, int n, int count) {
+  // exp(-2 pi i m / n) in FP64, reduced to the first octant-free form
+  // cos(2 pi m/n), -sin(2 pi m/n) with m taken mod n.
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int m = 0; m < count; ++m) {
+    long mm = m % n;
+    double ang = two_pi * (double)mm / (double)n;
+    v[off + m].x = (T)std::cos(ang);
+    v[off + m].y = (T)(-std::sin(ang));
+  }
+}
+
+template <typename T>
+int get_plan3(int nx, int ny, int nz, bool build, Plan3<T>* out) {
+  if (nx < 1 || ny < 1 || nz < 2 || (nz & 1))
+    return set_error(JLD_ERR_UNSUPPORTED, "FFT: mesh (%d,%d,%d) unsupported (need nz even >= 2)",
+                     nx, ny, nz);
+  int dev = 0;
+  JLD_CUDA_TRY(cudaGetDevice(&dev));
+  const int h = nz / 2;
+  auto key = std::make_tuple(dev, (int)sizeof(T), nx, ny, nz);
+  std::lock_guard<std::mutex> lock(g_plan_mu);
+  auto it = g_plans.find(key);
+  if (it == g_plans.end()) {
+    if (!build)
+      return set_error(JLD_ERR_NOPLAN,
+                       "FFT plan for (%d,%d,%d) missing; call jld_buildplan before stream capture",
+                       nx, ny, nz);
+    PlanEntry e;
+    const int lens[3] = {nx, ny, h};
+    for (int a = 0; a < 3; ++a)
+      if (!make_line_schedule(lens[a], &e.E[a], &e.nst[a], e.radix[a]))
+        return set_error(JLD_ERR_UNSUPPORTED,
+                         "FFT: length %d does not factor into 2, 3 and 5", lens[a]);
+    e.off[0] = 0;
+    e.off[1] = e.off[0] + nx;
+    e.off[2] = e.off[1] + ny;
+    e.off[3] = e.off[2] + h;
+    size_t total = e.off[3] + h + 1;
+    std::vector<cplx_t<T>> host(total);
+    fill_twiddles<T>(host, e.off[0], nx, nx);
+    fill_twiddles<T>(host, e.off[1], ny, ny);
+    fill_twiddles<T>(host, e.off[2], h, h);
+    fill_twiddles<T>(host, e.off[3], nz, h + 1);
+    JLD_CUDA_TRY(cudaMalloc(&e.dev, total * sizeof(cplx_t<T>)));
+    JLD_CUDA_TRY(cudaMemcpy(e.dev, host.data(), total * sizeof(cplx_t<T>),
+                            cudaMemcpyHostToDevice));
+    it = g_plans.emplace(key, e).first;
+  }
+  const PlanEntry& e = it->second;
+  const cplx_t<T>* base = (const cplx_t<T>*)e.dev;
+  out->nx = nx; out->ny = ny; out->nz = nz; out->h = h;
+  LinePlan<T>* lp[3] = {&out->px, &out->py, &out->pz};
+  const int lens[3] = {nx, ny, h};
+  for (int a = 0; a < 3; ++a) {
+    lp[a]->n = lens[a];
+    lp[a]->E = e.E[a];
+    lp[a]->nst = e.nst[a];
+    for (int s = 0; s < kMaxStages; ++s) lp[a]->radix[s] = s < e.nst[a] ? e.radix[a][s] : 0;
+    lp[a]->tw = base + e.off[a];
+  }
+  out->twr = base + e.off[3];
+  return JLD_OK;
+}
+
+template int get_plan3<float>(int, int, int, bool, Plan3<float>*);
+template int get_plan3<double>(int, int, int, bool, Plan3<double>*);
+
+// Returns the plan for an FFT call: built on demand unless the stream is
+// being captured into a CUDA graph (plan building allocates and copies).
+template <typename T>
+static int plan_for_call(cudaStream_t st, int nx, int ny, int nz, Plan3<T>* pl) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  JLD_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  return get_plan3<T>(nx, ny, nz, cs == cudaStreamCaptureStatusNone, pl);
+}
+
+// ---------------------------------------------------------------------------
+// Full transforms.
+
+template <typename T>
+static int fft_args_check(int nx, int ny, int nz, const void* ws, size_t ws_bytes,
+                          const char* who) {
+  if (nx < 1 || ny < 1 || nz < 2)
+    return set_error(JLD_ERR_ARG, "%s: mesh sizes must be positive (nz >= 2)", who);
+  if (nz & 1) return set_error(JLD_ERR_UNSUPPORTED, "%s: nz must be even", who);
+  size_t need = (size_t)nx * ny * (nz / 2 + 1) * sizeof(cplx_t<T>);
+  if (!ws || ws_bytes < need)
+    return set_error(JLD_ERR_WORKSPACE, "%s: workspace of %zu bytes needed, got %zu", who,
+                     need, ws ? ws_bytes : (size_t)0);
+  return JLD_OK;
+}
+
+// r2c: data (nx,ny,nz) real -> out in caller layout (interleaved, or split
+// when out_c == nullptr).
+template <typename T>
+static int rfft3(cudaStream_t st, const T* data, int nx, int ny, int nz, cplx_t<T>* out_c,
+                 T* out_re, T* out_im, void* ws, size_t ws_bytes, const char* who) {
+  int s = fft_args_check<T>(nx, ny, nz, ws, ws_bytes, who);
+  if (s) return s;
+  if (!data || (!out_c && (!out_re || !out_im)))
+    return set_error(JLD_ERR_ARG, "%s: NULL data or output", who);
+  Plan3<T> pl;
+  if ((s = plan_for_call<T>(st, nx, ny, nz, &pl))) return s;
+  const int h = pl.h;
+  cplx_t<T>* main = (cplx_t<T>*)ws;
+  cplx_t<T>* nyq = main + (size_t)nx * ny * h;
+  if ((s = launch_rfft_z<T>(st, pl, data, nullptr, main, nyq))) return s;
+  if ((s = launch_y_pass<T>(st, pl, main, nyq, -1))) return s;
+  // x pass: internal -> caller layout (row length h+1)
+  LineJob<T> jm = job_x_internal<T>(pl, main, false);
+  LineJob<T> jn = job_x_internal<T>(pl, nyq, true);
+  set_job_out_ref<T>(jm, pl, false, out_c, out_re, out_im);
+  set_job_out_ref<T>(jn, pl, true, out_c, out_re, out_im);
+  return launch_line_pass<T>(st, pl.px, jm, jn, -1);
+}
+
+template <typename T>
+static int irfft3(cudaStream_t st, const cplx_t<T>* in_c, const T* in_re, const T* in_im,
+                  int nx, int ny, int nz, T* out, void* ws, size_t ws_bytes, const char* who) {
+  int s = fft_args_check<T>(nx, ny, nz, ws, ws_bytes, who);
+  if (s) return s;
+  if (!out || (!in_c && (!in_re || !in_im)))
+    return set_error(JLD_ERR_ARG, "%s: NULL input or output", who);
+  Plan3<T> pl;
+  if ((s = plan_for_call<T>(st, nx, ny, nz, &pl))) return s;
+  const int h = pl.h;
+  cplx_t<T>* main = (cplx_t<T>*)ws;
+  cplx_t<T>* nyq = main + (size_t)nx * ny * h;
+  LineJob<T> jm = job_x_internal<T>(pl, main, false);
+  LineJob<T> jn = job_x_internal<T>(pl, nyq, true);
+  set_job_in_ref<T>(jm, pl, false, in_c, in_re, in_im);
+  set_job_in_ref<T>(jn, pl, true, in_c, in_re, in_im);
+  if ((s = launch_line_pass<T>(st, pl.px, jm, jn, +1))) return s;
+  if ((s = launch_y_pass<T>(st, pl, main, nyq, +1))) return s;
+  return launch_irfft_z<T>(st, pl, main, nyq, out);
+}
+
+}  // namespace jld
+
+using namespace jld;
+#define ST(s) reinterpret_cast<cudaStream_t>(s)
+
+extern "C" {
+
+int jld_buildplan_f32(int32_t nx, int32_t ny, int32_t nz, int32_t local_out[2]) {
+  clear_error();
+  Plan3<float> pl;
+  int s = get_plan3<float>(nx, ny, nz, true, &pl);
+  if (s) return s;
+  if (local_out) { local_out[0] = nx; local_out[1] = 0; }
+  return JLD_OK;
+}
+int jld_buildplan_f64(int32_t nx, int32_t ny, int32_t nz, int32_t local_out[2]) {
+  clear_error();
+  Plan3<double> pl;
+  int s = get_plan3<double>(nx, ny, nz, true, &pl);
+  if (s) return s;
+  if (local_out) { local_out[0] = nx; local_out[1] = 0; }
+  return JLD_OK;
+}
+size_t jld_fft_workspace_f32(int32_t nx, int32_t ny, int32_t nz) {
+  if (nx < 1 || ny < 1 || nz < 2) return 0;
+  return (size_t)nx * ny * (nz / 2 + 1) * sizeof(float2);
+}
+size_t jld_fft_workspace_f64(int32_t nx, int32_t ny, int32_t nz) {
+  if (nx < 1 || ny < 1 || nz < 2) return 0;
+  return (size_t)nx * ny * (nz / 2 + 1) * sizeof(double2);
+}
+
+int jld_pfft_f32(jld_stream_t s, const float* data, int32_t nx, int32_t ny, int32_t nz,
+                 float* re, float* im, void* ws, size_t wsb) {
+  clear_error();
+  return rfft3<float>(ST(s), data, nx, ny, nz, nullptr, re, im, ws, wsb, "jld_pfft_f32");
+}
+int jld_pfft_f64(jld_stream_t s, const double* data, int32_t nx, int32_t ny, int32_t nz,
+                 double* re, double* im, void* ws, size_t wsb) {
+  clear_error();
+  return rfft3<double>(ST(s), data, nx, ny, nz, nullptr, re, im, ws, wsb, "jld_pfft_f64");
+}
+int jld_pfft_c_f32(jld_stream_t s, const float* data, int32_t nx, int32_t ny, int32_t nz,
+                   void* out, void* ws, size_t wsb) {
+  clear_error();
+  return rfft3<float>(ST(s), data, nx, ny, nz, (float2*)out, nullptr, nullptr, ws, wsb,
+                      "jld_pfft_c_f32");
+}
+int jld_pfft_c_f64(jld_stream_t s, const double* data, int32_t nx, int32_t ny, int32_t nz,
+                   void* out, void* ws, size_t wsb) {
+  clear_error();
+  return rfft3<double>(ST(s), data, nx, ny, nz, (double2*)out, nullptr, nullptr, ws, wsb,
+                       "jld_pfft_c_f64");
+}
+int jld_pifft_f32(jld_stream_t s, const float* re, const float* im, int32_t nx, int32_t ny,
+                  int32_t nz, float* out, void* ws, size_t wsb) {
+  clear_error();
+  return irfft3<float>(ST(s), nullptr, re, im, nx, ny, nz, out, ws, wsb, "jld_pifft_f32");
+}
+int jld_pifft_f64(jld_stream_t s, const double* re, const double* im, int32_t nx, int32_t ny,
+                  int32_t nz, double* out, void* ws, size_t wsb) {
+  clear_error();
+  return irfft3<double>(ST(s), nullptr, re, im, nx, ny, nz, out, ws, wsb, "jld_pifft_f64");
+}
+int jld_pifft_c_f32(jld_stream_t s, const void* in, int32_t nx, int32_t ny, int32_t nz,
+                    float* out, void* ws, size_t wsb) {
+  clear_error();
+  return irfft3<float>(ST(s), (const float2*)in, nullptr, nullptr, nx, ny, nz, out, ws, wsb,
+                       "jld_pifft_c_f32");
+}
+int jld_pifft_c_f64(jld_stream_t s, const void* in, int32_t nx, int32_t ny, int32_t nz,
+                    double* out, void* ws, size_t wsb) {
+  clear_error();
+  return irfft3<double>(ST(s), (const double2*)in, nullptr, nullptr, nx, ny, nz, out, ws, wsb,
+                        "jld_pifft_c_f64");
+}
+
+}  // extern "C"

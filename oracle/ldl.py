@@ -1,0 +1,229 @@
+"""ORACLE — test infrastructure only.  FP64 restatement of the LDL pipeline
+and of its gradient, used by tests/, the smoke check and bench.py's CPU
+baseline as the checker.
+
+Forward (model.py): per layer (model.py:186-212 "sm", 137-179 "dm")
+    rho   = paint(X, 1) * fact                    fact = prod(Nmesh) / Npart
+    s     = (rho + 1e-8) ** gamma
+    shat  = pfft(s) / prod(Nmesh)                 (pmesh.py:112)
+    G     = -exp(-k^2/kl^2 - kh^2/k^2) k^nu       ("sm";  "dm": -exp(-k/kl - kh/k) k^nu)
+    P     = 1e-2 * alpha * shat * G
+    g_d   = pifft(-1j * c_d(k) * P),  c_d = (45 sin(k h) - 9 sin(2kh) + sin(3kh)) / (30 h)
+    X    += stack(readout(X, g_d))
+final paint and bias (model.py:311, 344): F = ReLU(w (rho + 1e-8)^mu + b),
+loss (model.py:373-403): sum(mask |F - target|^{1|2}) / Npixel.
+Wavevectors (pmesh.py:175-186): k_d = 2 pi fftfreq(N_d, L_d/N_d), kz cut to
+[0, Nz/2] (so the Nyquist plane carries the negative frequency), |k| = 0
+replaced by 1e-8 (model.py:101-102).
+
+Gradient, two modes:
+  "reference": the composition of the reference's custom VJP rules as JAX
+      applies them (jaxpops_bind.py:236-247, 351-363, 699-701, 758-759;
+      model.py:23-29), with JAX's cotangent convention dL/dRe - i dL/dIm.
+      pifft's rule omits the half-spectrum multiplicity m_k (2 for
+      0 < kz < Nz/2), so d loss / d alpha is biased.
+  "true": the exact adjoint: pifft's adjoint carries m_k, pfft's adjoint
+      sums the half spectrum once, c2f's rule is the identity.
+Both modes agree except in d/d alpha (on cubic meshes).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import cic
+from .fft import pfft, pifft
+
+PARAMS_PER_LAYER = 5  # alpha, gamma, kh, kl, nu (model.py:268-272)
+
+
+def fftfreq_signed(n: int) -> np.ndarray:
+    """Integer frequency index of numpy's fftfreq ordering."""
+    return np.fft.fftfreq(n, 1.0 / n)
+
+
+@dataclass
+class LDLOracle:
+    nmesh: tuple
+    box: tuple
+    kind: str = "sm"
+    L1: bool = True
+    cache: dict = field(default_factory=dict)
+
+    def __post_init__(self):
+        self.nmesh = tuple(int(v) for v in np.broadcast_to(np.asarray(self.nmesh), (3,)))
+        self.box = tuple(float(v) for v in np.broadcast_to(np.asarray(self.box, dtype=float), (3,)))
+        N, L = self.nmesh, self.box
+        ks = []
+        for a in range(3):
+            k = np.fft.fftfreq(N[a], L[a] / N[a]) * 2 * np.pi
+            if a == 2:
+                k = k[: N[2] // 2 + 1]
+            ks.append(k)
+        KX, KY, KZ = np.meshgrid(*ks, indexing="ij")
+        self.kvec = (KX, KY, KZ)
+        kn = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
+        self.knorm = np.where(kn == 0, 1e-8, kn)
+        step = np.array(L) / np.array(N)
+        self.coeff = [1.0 / (30 * step[a]) * (45 * np.sin(self.kvec[a] * step[a])
+                                               - 9 * np.sin(2 * self.kvec[a] * step[a])
+                                               + np.sin(3 * self.kvec[a] * step[a])) for a in range(3)]
+        # half-spectrum multiplicity along z
+        h = N[2] // 2 + 1
+        m = np.full(h, 2.0)
+        m[0] = 1.0
+        if N[2] % 2 == 0:
+            m[-1] = 1.0
+        self.mult = m[None, None, :]
+        self.ncell = float(np.prod(N))
+
+    # -- pieces ---------------------------------------------------------------
+    def mesh_pos(self, X):
+        return cic.box_to_mesh(np.asarray(X, dtype=np.float64), self.box, self.nmesh)
+
+    def green(self, kh, kl, nu):
+        k = self.knorm
+        if self.kind == "dm":
+            return -np.exp(-k / kl - kh / k) * k ** nu
+        return -np.exp(-k ** 2 / kl ** 2 - kh ** 2 / k ** 2) * k ** nu
+
+    def green_grads(self, G, kh, kl, nu):
+        """dG/dkh, dG/dkl, dG/dnu."""
+        k = self.knorm
+        if self.kind == "dm":
+            return G * (-1.0 / k), G * (k / kl ** 2), G * np.log(k)
+        return G * (-2.0 * kh / k ** 2), G * (2.0 * k ** 2 / kl ** 3), G * np.log(k)
+
+    # -- forward --------------------------------------------------------------
+    def layer_forward(self, X, prm, fact):
+        alpha, gamma, kh, kl, nu = prm
+        Xm = self.mesh_pos(X)
+        rho = cic.paint(Xm, 1.0, self.nmesh) * fact
+        s = (rho + 1e-8) ** gamma
+        shat = pfft(s) / self.ncell
+        G = self.green(kh, kl, nu)
+        P = 1e-2 * alpha * shat * G
+        g = [pifft(-1j * self.coeff[d] * P, self.nmesh) for d in range(3)]
+        disp = np.stack([cic.readout(Xm, g[d], self.nmesh, self.box) for d in range(3)], axis=-1)
+        c = dict(Xm=Xm, rho=rho, s=s, shat=shat, G=G, g=g, prm=prm)
+        return X + disp, c
+
+    def final_map(self, X, mu, w, b, fact):
+        Xm = self.mesh_pos(X)
+        rho = cic.paint(Xm, 1.0, self.nmesh) * fact
+        if self.kind == "dm":
+            return rho, dict(Xm=Xm, rho=rho)
+        base = (rho + 1e-8) ** mu
+        u = w * base + b
+        F = np.where(u > 1e-12, u, 1e-12)
+        return F, dict(Xm=Xm, rho=rho, base=base, u=u)
+
+    def forward(self, params, X, target, nstep, mask=None):
+        params = np.asarray(params, dtype=np.float64)
+        X = np.asarray(X, dtype=np.float64)
+        fact = self.ncell / len(X)
+        layers = []
+        for l in range(nstep):
+            X, c = self.layer_forward(X, params[5 * l: 5 * l + 5], fact)
+            layers.append(c)
+        if self.kind == "dm":
+            mu = w = b = 0.0
+        else:
+            mu, w, b = params[5 * nstep: 5 * nstep + 3]
+        F, fc = self.final_map(X, mu, w, b, fact)
+        diff = F - target
+        ad = np.abs(diff)
+        if mask is not None:
+            ad = ad * mask
+            npix = float(np.sum(mask))
+        else:
+            npix = float(diff.size)
+        loss = (np.sum(ad) if self.L1 else np.sum(ad ** 2)) / npix
+        self.cache = dict(layers=layers, final=fc, F=F, diff=diff, mask=mask, npix=npix,
+                          fact=fact, params=params, nstep=nstep, X_final=X)
+        return float(loss)
+
+    # -- backward -------------------------------------------------------------
+    def backward(self, mode="reference"):
+        """Gradient of the last forward() loss w.r.t. the parameter vector."""
+        if mode not in ("reference", "true"):
+            raise ValueError("mode must be 'reference' or 'true'")
+        c = self.cache
+        params, nstep, fact = c["params"], c["nstep"], c["fact"]
+        grad = np.zeros_like(params)
+        diff, mask, npix = c["diff"], c["mask"], c["npix"]
+        m = mask if mask is not None else 1.0
+        # d|diff|/d diff with JAX's abs rule (+1 at zero)
+        sgn = np.where(diff >= 0, 1.0, -1.0)
+        if self.L1:
+            ctF = sgn * m / npix
+        else:
+            ctF = 2.0 * np.abs(diff) * m * m * sgn / npix
+        fc = c["final"]
+        if self.kind == "dm":
+            ct_rho = ctF
+        else:
+            mu, w, b = params[5 * nstep: 5 * nstep + 3]
+            ctu = ctF * (fc["u"] > 1e-12)
+            lr = np.log(fc["rho"] + 1e-8)
+            grad[5 * nstep + 0] = np.sum(ctu * w * fc["base"] * lr)
+            grad[5 * nstep + 1] = np.sum(ctu * fc["base"])
+            grad[5 * nstep + 2] = np.sum(ctu)
+            ct_rho = ctu * w * mu * (fc["rho"] + 1e-8) ** (mu - 1)
+        Xbar = cic.readout3d(fc["Xm"], ct_rho * fact, self.nmesh, self.box, vjp=True)
+        for l in reversed(range(nstep)):
+            Xbar, g5 = self.layer_backward(c["layers"][l], Xbar, fact, mode)
+            grad[5 * l: 5 * l + 5] = g5
+        return grad
+
+    def layer_backward(self, lc, Xbar_next, fact, mode):
+        alpha, gamma, kh, kl, nu = lc["prm"]
+        Xm, g = lc["Xm"], lc["g"]
+        Xbar = Xbar_next.copy()
+        ct_g = []
+        for d in range(3):
+            v = Xbar_next[:, d]
+            Xbar += cic.readout3d(Xm, g[d], self.nmesh, self.box, vjp=True) * v[:, None]
+            ct_g.append(cic.paint(Xm, v, self.nmesh))
+        ctP = np.zeros_like(lc["shat"])
+        for d in range(3):
+            ctV = np.conj(pfft(ct_g[d]))
+            if mode == "true":
+                ctV = ctV * self.mult
+            ctP += (-1j * self.coeff[d]) * ctV
+        shat, G = lc["shat"], lc["G"]
+        ctw = G * ctP                                   # w = 1e-2 alpha shat
+        ctG = np.real(ctP * (1e-2 * alpha * shat))
+        if mode == "reference":                          # c2f rule, model.py:23-29
+            sz = ctG.shape[1]
+            ctG[:, :, 1:sz // 2] *= 2.0
+        g_alpha = 1e-2 * np.sum(np.real(ctw * shat))
+        dkh, dkl, dnu = self.green_grads(G, kh, kl, nu)
+        g_kh, g_kl, g_nu = np.sum(ctG * dkh), np.sum(ctG * dkl), np.sum(ctG * dnu)
+        ctF = (1e-2 * alpha) * ctw / self.ncell
+        if mode == "reference":
+            cts = pifft(np.conj(ctF), self.nmesh)
+        else:
+            cts = pifft(np.conj(ctF) / self.mult, self.nmesh)
+        rho, s = lc["rho"], lc["s"]
+        g_gamma = np.sum(cts * s * np.log(rho + 1e-8))
+        ct_rho = cts * gamma * (rho + 1e-8) ** (gamma - 1)
+        Xbar += cic.readout3d(Xm, ct_rho * fact, self.nmesh, self.box, vjp=True)
+        return Xbar, np.array([g_alpha, g_gamma, g_kh, g_kl, g_nu])
+
+    def loss_and_grad(self, params, X, target, nstep, mask=None, mode="reference"):
+        loss = self.forward(params, X, target, nstep, mask)
+        return loss, self.backward(mode)
+
+    def fd_grad(self, params, X, target, nstep, mask=None, step=1e-3, idx=None):
+        """Central finite differences of the loss, step `step` per parameter."""
+        params = np.asarray(params, dtype=np.float64)
+        idx = range(len(params)) if idx is None else idx
+        out = np.full(len(params), np.nan)
+        for i in idx:
+            p1 = params.copy(); p1[i] += step
+            p0 = params.copy(); p0[i] -= step
+            out[i] = (self.forward(p1, X, target, nstep, mask) -
+                      self.forward(p0, X, target, nstep, mask)) / (2 * step)
+        return out
