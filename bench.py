@@ -1,0 +1,390 @@
+"""LDL forward+adjoint benchmark on one GB300 (or N replicas under torchrun).
+
+Workload (default, the 512^3 configuration of the metric): clustered 512^3
+particles on a 512^3 mesh -- a Zel'dovich lattice with 3-cell rms
+displacement plus 10% extra particles in 2000 Gaussian halos of 0.5-cell
+width with Poisson counts -- two "sm" displacement layers (alpha, gamma, kh,
+kl, nu) = (0.05, 1, 0.5, 2, 1), the ReLU bias map (mu, w, b) = (1.5, 1, -0.1),
+L1 loss against the model's own output times lognormal noise (sigma 0.1).
+Seeded synthetic data; box = 100 * n / 64 (the 64^3 configuration's cell
+size).
+
+A step is one fused, CUDA-graph-captured forward + adjoint evaluation
+(loss and all 13 parameter gradients) with inputs resident in HBM.  The
+inputs (1.8 GB of positions, 0.5 GB target) exceed the 129 MB L2, so no
+flush is needed between steps.  `e2e` repeats the step through the public
+API with host buffers: pinned-host -> device copies of positions and target
+and a device -> host read of loss and gradients inside the timed region.
+
+--impl reference times the oracle's CPU restatement of the same step (C CIC
+loops, pocketFFT) on a bounded sample (a 128^3 version of the workload),
+scaled to the 512^3 workload by particle count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() \
+    else "LDL fwd+grad steps/s at 512^3"
+UNIT = "steps/s"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+def make_workload(n: int, device, seed: int = 0):
+    import torch
+    from jerald_gb300 import synth
+    box = 100.0 * n / 64
+    pos = synth.clustered(n, box, seed=seed, device=device)
+    return pos.contiguous(), box
+
+
+def make_target(pos, n, box, params, device):
+    import torch
+    from jerald_gb300 import synth
+    from jerald_gb300.model import JERALDModel
+    from jerald_gb300.pmesh import PMesh
+    pm = PMesh(n, box, device=device, dtype=torch.float32)
+    model = JERALDModel(pos, None, pm, Nstep=2, kind="sm")
+    with torch.no_grad():
+        F = model.evaluate(torch.as_tensor(params, dtype=torch.float32, device=device), pos, 2)
+    noise = torch.from_numpy(synth.lognormal_noise(F.shape, 0.1, seed=2).astype(np.float32)).to(device)
+    return (F * noise).contiguous()
+
+
+def time_primitives(pos, n, box, steps, warmup):
+    """Per-kernel CUDA-event timings of the drop-in primitives on the workload,
+    with algorithmic bytes (12N + 4C paint, 16N + 4C readout, 4C + 8H r2c)."""
+    import ctypes as ct
+    import torch
+    from jerald_gb300 import _lib
+    N = pos.shape[0]
+    C = n ** 3
+    H = n * n * (n // 2 + 1)
+    b = np.asarray([box] * 3, dtype=np.float32)
+    mesh = torch.empty((n, n, n), device=pos.device)
+    out = torch.empty(N, device=pos.device)
+    spec = torch.empty((n, n, n // 2 + 1), dtype=torch.complex64, device=pos.device)
+    ws = torch.empty(int(_lib.load().jld_fft_workspace_f32(n, n, n)), dtype=torch.uint8, device=pos.device)
+    field = torch.randn((n, n, n), device=pos.device)
+    st = torch.cuda.current_stream()
+    sp = ct.c_void_p(st.cuda_stream)
+    P = lambda t: ct.c_void_p(t.data_ptr())  # noqa: E731
+    bp = b.ctypes.data_as(ct.c_void_p)
+    ops = {
+        "paint": (lambda: _lib.call("jld_ppaint_box_f32", sp, P(pos), N, None, ct.c_float(1.0), n, n, n, bp, P(mesh)),
+                  12 * N + 4 * C),
+        "readout": (lambda: _lib.call("jld_preadout_box_f32", sp, P(pos), N, P(field), n, n, n, bp, -1, P(out)),
+                    16 * N + 4 * C),
+        "r2c": (lambda: _lib.call("jld_pfft_c_f32", sp, P(field), n, n, n, P(spec), P(ws), ws.numel()),
+                4 * C + 8 * H),
+    }
+    res = {}
+    for name, (fn, nbytes) in ops.items():
+        for _ in range(warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(steps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res[name] = {"ms": ms, "algorithmic_bytes": int(nbytes), "gbs": nbytes / ms / 1e6}
+    return res
+
+
+def count_launches(nstep: int, kind: str, mask: bool) -> int:
+    fwd = 7 * nstep
+    final = 1 + (1 if mask else 0) + 1 + 1 + (2 if kind == "sm" else 1) + 1
+    bwd = 9 * nstep
+    return fwd + final + bwd
+
+
+def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int | None = None):
+    """Times the oracle's 2-layer fwd+grad at n_sample^3 (clustered recipe)."""
+    from jerald_gb300 import synth
+    from oracle import fft as offt
+    from oracle.ldl import LDLOracle
+    threads = threads or os.cpu_count() or 1
+    offt.set_workers(threads)
+    box = 100.0 * n_sample / 64
+    X = synth.clustered(n_sample, box, seed=0).astype(np.float64)
+    p = synth.default_params(2)
+    o = LDLOracle((n_sample,) * 3, box, kind="sm", L1=True)
+    o.forward(p, X, np.ones((n_sample,) * 3), 2)
+    tgt = o.cache["F"] * synth.lognormal_noise(o.cache["F"].shape, 0.1, 2)
+    o.loss_and_grad(p, X, tgt, 2)  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.loss_and_grad(p, X, tgt, 2)
+    dt = (time.perf_counter() - t0) / steps
+    n_part_sample = len(X)
+    n_part_full = int(round(1.1 * n_full ** 3))
+    value = (1.0 / dt) * n_part_sample / n_part_full
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle 2-layer fwd+grad at {n_sample}^3 ({n_part_sample} particles, "
+                      f"{dt:.2f} s/step; CIC loops single-threaded C, FFT pocketfft with {threads} workers), "
+                      f"scaled by particle count to {n_full}^3"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n_full = args.n
+    n_sample = max(16, min(128, n_full))
+    cb = cpu_baseline_sample(n_sample, n_full, steps=1)
+    vals = []
+    from jerald_gb300 import synth  # noqa: F401
+    for _ in range(args.warmup):
+        pass
+    for _ in range(args.steps):
+        r = cpu_baseline_sample(n_sample, n_full, steps=1)
+        vals.append(r["value"])
+    v = float(np.median(vals)) if vals else cb["value"]
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": f"clustered {n_full}^3 particles+10% halos, {n_full}^3 mesh, 2 sm layers",
+                       "nmesh": n_full},
+            "cpu_baseline": {**cb, "value": v},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512, help="mesh size per axis (workload scale)")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain primitive path")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+
+    n = args.n
+    params = synth.default_params(2)
+    pos, box = make_workload(n, dev, seed=rank)
+    target = make_target(pos, n, box, params, dev)
+    N = pos.shape[0]
+    step = FusedLDL(n, box, N, nstep=2, kind="sm", L1=True, grad_mode="reference", device=dev)
+    step(pos, params, target)
+    step.capture(pos, target)
+    for _ in range(args.warmup):
+        step.replay(params)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    st = torch.cuda.current_stream(dev)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            step.replay(params)
+        e1.record(st)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+    loss, grad = step.out[0].item(), step.out[1:].cpu().numpy()
+
+    # e2e: host buffers -> device, step, loss+grads -> host
+    pos_h = pos.cpu().pin_memory()
+    tgt_h = target.cpu().pin_memory()
+    out_h = torch.empty(step.out.shape, dtype=torch.float64).pin_memory()
+    h2d = pos_h.numel() * 4 + tgt_h.numel() * 4
+    d2h = out_h.numel() * 8
+    for _ in range(args.warmup):
+        pos.copy_(pos_h, non_blocking=True)
+        target.copy_(tgt_h, non_blocking=True)
+        step.replay(params)
+        out_h.copy_(step.out, non_blocking=True)
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(st)
+    for _ in range(args.steps):
+        pos.copy_(pos_h, non_blocking=True)
+        target.copy_(tgt_h, non_blocking=True)
+        step.replay(params)
+        out_h.copy_(step.out, non_blocking=True)
+    e3.record(st)
+    barrier()
+    ms_e2e = e2.elapsed_time(e3) / args.steps
+    if world > 1:
+        t = torch.tensor([ms_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+
+    extra = {}
+    peak, peak_kind = _peaks()
+    kern = time_primitives(pos, n, box, steps=5, warmup=3) if rank == 0 else {}
+    prof = ROOT / "profiles" / "traffic.json"
+    traffic = json.loads(prof.read_text()) if prof.exists() else {}
+    dominant = "paint"
+    dk = kern.get(dominant, {"gbs": 0.0, "algorithmic_bytes": 0})
+    roofline = {"bound": "hbm", "achieved": dk["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": dk["gbs"] / peak, "traffic": traffic.get(dominant, {}).get("bytes_per_launch_full"),
+                "kernel": dominant, "peak_kind": peak_kind,
+                "kernels": {k: {"gbs": v["gbs"], "frac": v["gbs"] / peak, "ms": v["ms"]} for k, v in kern.items()}}
+
+    if not args.no_plain and rank == 0:
+        from jerald_gb300.model import JERALDModel
+        from jerald_gb300.pmesh import PMesh
+        pm = PMesh(n, box, device=dev, dtype=torch.float32)
+        model = JERALDModel(pos, target, pm, Nstep=2, kind="sm")
+        pt = torch.as_tensor(params, dtype=torch.float32)
+        lp, gp = model.loss_and_grad(pt)
+        torch.cuda.synchronize()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record(st)
+        kp = 3
+        for _ in range(kp):
+            lp, gp = model.loss_and_grad(pt)
+        e5.record(st)
+        torch.cuda.synchronize()
+        plain_ms = e4.elapsed_time(e5) / kp
+        gp = gp.cpu().numpy()
+        extra["plain_ms_per_step"] = plain_ms
+        extra["speedup_vs_plain"] = plain_ms / ms
+        rel = np.abs(grad - gp) / np.maximum(np.abs(gp), 1e-6 * np.abs(gp).max())
+        extra["grad_rel_diff_vs_plain"] = float(rel.max())
+        extra["loss_rel_diff_vs_plain"] = abs(loss - float(lp)) / abs(float(lp))
+        del model, pm
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        try:
+            cpu = cpu_baseline_sample(min(128, n), n, steps=1)
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Zel'dovich lattice + Gaussian halos)",
+                "config": {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, 2 sm layers + "
+                                       f"ReLU map, L1 loss, fwd+adjoint (13 grads), graph-captured",
+                           "nmesh": n, "nparts": N, "box": box, "nstep": 2, "kind": "sm",
+                           "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1
+                           else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": world * 1000.0 / ms_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+                "gpu_launches": count_launches(2, "sm", False) * args.steps,
+                "clocks": clk.summary(), "loss": loss, **extra}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

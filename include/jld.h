@@ -209,6 +209,39 @@ JLD_API int jld_pifft_c_f32(jld_stream_t stream, const void* in_c, int32_t nx, i
 JLD_API int jld_pifft_c_f64(jld_stream_t stream, const void* in_c, int32_t nx, int32_t ny,
                     int32_t nz, double* out, void* ws, size_t ws_bytes);
 
+/* ------------------------------------------------------------------ */
+/* Fused LDL step: forward of `nstep` displacement layers, final map and  */
+/* loss, and the adjoint, in one stream-ordered call.  It computes what   */
+/* the reference's model.py evaluates through jaxpops_bind (loss at        */
+/* model.py:351-403, its gradient through value_and_grad at 410-413), for  */
+/* kind 0 = "sm" (potential_gradient_sm, model.py:186-212, ReLU bias map   */
+/* model.py:338-344) and kind 1 = "dm" (model.py:137-179, 346-347).        */
+/*   pos     (nparts, 3) float32 box-unit positions (device)               */
+/*   params  device float32: 5 per layer (alpha, gamma, kh, kl, nu),      */
+/*           then (mu, w, b) for kind 0                                    */
+/*   target  (nx, ny, nz) device float32; mask the same or NULL            */
+/*   L1      1: sum |F - target| (model default for "sm"), 0: squares      */
+/*   grad_mode 0: the reference's VJP rules, 1: exact adjoint (differs    */
+/*           from 0 only in d/d alpha)                                     */
+/*   paint_method 0: atomics, 1: warp-aggregated atomics                   */
+/*   out     device float64: [loss, d loss / d params ...]                 */
+/* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
+/* into a CUDA graph; parameters are read from device memory, so a graph  */
+/* replays with whatever `params` holds.                                  */
+JLD_API size_t jld_ldl_workspace_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                                     int32_t nstep);
+JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float box[3]);
+JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                             int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                             int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
+                             int32_t paint_method, const float* params, const float* target,
+                             const float* mask, void* ws, size_t ws_bytes, double* out);
+/* Device pointer to the positions after `layer` (1..nstep) layers of the */
+/* last step run on `ws`.                                                  */
+JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,
+                                  int64_t nparts, int32_t nstep, int32_t layer,
+                                  const float** out);
+
 #ifdef __cplusplus
 }
 #endif

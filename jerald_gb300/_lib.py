@@ -55,6 +55,10 @@ _SIGS = {
     "jld_pifft_f64": [_c_void_p, _c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
     "jld_pifft_c_f32": [_c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
     "jld_pifft_c_f64": [_c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
+    "jld_ldl_prepare_f32": [_i32, _i32, _i32, _c_void_p],
+    "jld_ldl_step_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32, _i32,
+                         _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
+    "jld_ldl_positions_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _i32, _c_void_p],
 }
 _RESTYPES = {
     "jld_version": ct.c_char_p,
@@ -62,8 +66,10 @@ _RESTYPES = {
     "jld_last_error": ct.c_char_p,
     "jld_fft_workspace_f32": _size,
     "jld_fft_workspace_f64": _size,
+    "jld_ldl_workspace_f32": _size,
 }
 _EXTRA_ARGS = {
+    "jld_ldl_workspace_f32": [_i32, _i32, _i32, _i64, _i32],
     "jld_status_string": [ct.c_int],
     "jld_fft_workspace_f32": [_i32, _i32, _i32],
     "jld_fft_workspace_f64": [_i32, _i32, _i32],

@@ -351,6 +351,11 @@ static int readout3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T*
   return JLD_OK;
 }
 
+int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny,
+                   int64_t nz, const float* box, int method, float* out) {
+  return paint_impl<float>(st, pos, n, nullptr, 1.0f, nx, ny, nz, box, method, out, "fused paint");
+}
+
 template <typename T>
 static int keys_impl(cudaStream_t st, const T* pos, int64_t nparts, int64_t nx, int64_t ny,
                      int64_t nz, const T* box, int32_t* keys, const char* who) {

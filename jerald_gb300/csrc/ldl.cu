@@ -1,0 +1,337 @@
+// Host orchestration and C ABI of the fused LDL forward + adjoint step
+// (kernels in ldl_kernels.cuh).  One call runs the whole step on one stream:
+// ~9 launches per layer forward, ~9 per layer adjoint and 6 for the final
+// map, all stream-ordered and free of host synchronisation, so the step can
+// be captured into a CUDA graph once plans and tables exist
+// (jld_ldl_prepare_f32).
+
+#include <algorithm>
+
+#include "ldl_kernels.cuh"
+
+namespace jld {
+
+struct LdlLayout {
+  int64_t N, C, H;
+  int nstep;
+  size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
+      off_npix, total;
+  int64_t part_doubles;
+};
+
+static size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+static constexpr int kMaxCellBlocks = 8192;
+
+static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
+  LdlLayout L;
+  const int64_t h = nz / 2;
+  L.N = N; L.nstep = nstep;
+  L.C = (int64_t)nx * ny * nz;
+  L.H = (int64_t)nx * ny * (h + 1);
+  L.part_doubles = std::max<int64_t>({4 * ((int64_t)ny * (h + 1) + ny), (int64_t)nx * ny + 64,
+                                      4 * (int64_t)kMaxCellBlocks});
+  size_t o = 0;
+  L.off_pos = o; o += al(sizeof(float) * 3 * N * nstep);       // X_1 .. X_nstep
+  L.off_xb = o; o += al(sizeof(float) * 3 * N);                // cotangent of X (ping)
+  L.off_xb2 = o; o += al(sizeof(float) * 3 * N);               // (pong)
+  L.off_rho = o; o += al(sizeof(float) * L.C * (nstep + 1));   // unit-mass paint per layer + final
+  L.off_S = o; o += al(sizeof(float2) * L.H * nstep);          // FFT of the source per layer
+  L.off_g4 = o; o += al(sizeof(float4) * L.C * nstep);         // force mesh per layer
+  for (int i = 0; i < 5; ++i) { L.off_w[i] = o; o += al(sizeof(float2) * L.H); }
+  L.off_gb4 = o; o += al(sizeof(float4) * L.C);                // 3-channel cotangent mesh
+  L.off_rb = o; o += al(sizeof(float) * L.C);                  // density cotangent
+  L.off_part = o; o += al(sizeof(double) * L.part_doubles);    // per-block FP64 partials
+  L.off_npix = o; o += al(sizeof(double) * 2);                 // 1 / Npixel
+  L.total = o;
+  return L;
+}
+
+struct StepArgs {
+  cudaStream_t st;
+  const float* pos0; int64_t N;
+  int nx, ny, nz; float box[3];
+  int nstep, kind, L1, mode, paint_method;
+  const float* params;   // device: 5*nstep (+3 for kind 0)
+  const float* target; const float* mask;
+  char* ws;
+  double* out;           // device: [loss, grads...]
+};
+
+struct SpecGeom {
+  SpecPass sp;
+  int64_t tiles;
+  int nthr;
+  size_t smem1;  // one tile
+};
+
+static SpecGeom spec_geom(const LinePlan<float>& lp, int nx, int ny, int h, int ax, int ntiles_smem) {
+  SpecGeom g;
+  g.sp.nx = nx; g.sp.ny = ny; g.sp.h = h;
+  int cols = tile_cols(lp.n, lp.E, sizeof(float2));
+  while (cols > 1 && (size_t)lp.n * (cols + 1) * sizeof(float2) * ntiles_smem > 200 * 1024) cols >>= 1;
+  g.sp.cols = cols;
+  g.sp.cshift = ilog2i(cols);
+  const int64_t main_cols = ax == 0 ? (int64_t)ny * h : (int64_t)nx * h;
+  const int64_t nyq_cols = ax == 0 ? ny : nx;
+  g.sp.tiles_main = (main_cols + cols - 1) / cols;
+  g.tiles = g.sp.tiles_main + (nyq_cols + cols - 1) / cols;
+  g.nthr = cols * lp.n / lp.E;
+  g.smem1 = (size_t)lp.n * (cols + 1) * sizeof(float2);
+  return g;
+}
+
+static int ldl_step(const StepArgs& a) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz, h = nz / 2;
+  const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep);
+  cudaStream_t st = a.st;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  JLD_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  const bool may_build = cs == cudaStreamCaptureStatusNone;
+  Plan3<float> pl;
+  int s = get_plan3<float>(nx, ny, nz, may_build, &pl);
+  if (s) return s;
+  KTables kt;
+  if ((s = get_ktables(nx, ny, nz, a.box, may_build, &kt))) return s;
+  const Grid3 g = make_grid(nx, ny, nz);
+  BoxGeom bg;
+  const int nm[3] = {nx, ny, nz};
+  for (int i = 0; i < 3; ++i) {
+    bg.box[i] = a.box[i];
+    bg.cell[i] = a.box[i] / (float)nm[i];
+    bg.dw[i] = (float)nm[i] / a.box[i];
+  }
+  const float fact = (float)((double)L.C / (double)a.N);
+  const float scale = (float)(1.0 / (double)L.C);
+  char* ws = a.ws;
+  float* Xs = (float*)(ws + L.off_pos);
+  float* Xb = (float*)(ws + L.off_xb);
+  float* Xb2 = (float*)(ws + L.off_xb2);
+  float* rho = (float*)(ws + L.off_rho);
+  float2* Sbuf = (float2*)(ws + L.off_S);
+  float4* g4 = (float4*)(ws + L.off_g4);
+  float2* W[5];
+  for (int i = 0; i < 5; ++i) W[i] = (float2*)(ws + L.off_w[i]);
+  float4* gb4 = (float4*)(ws + L.off_gb4);
+  float* rb = (float*)(ws + L.off_rb);
+  double* part = (double*)(ws + L.off_part);
+  double* npix = (double*)(ws + L.off_npix);
+  const int64_t nyq_off = (int64_t)nx * ny * h;
+  auto Xl = [&](int l) -> const float* { return l == 0 ? a.pos0 : Xs + (size_t)3 * a.N * (l - 1); };
+  const int pblock = 256;
+  const unsigned pgrid = grid_for(a.N, pblock);
+  const int cblock = 256;
+  const unsigned cgrid = (unsigned)std::min<int64_t>(kMaxCellBlocks, grid_for(L.C, cblock));
+  const int64_t rows = (int64_t)nx * ny;
+
+  const SpecGeom gx = spec_geom(pl.px, nx, ny, h, 0, 2);
+  const SpecGeom gy = spec_geom(pl.py, nx, ny, h, 1, 2);
+  int zcols = tile_cols(pl.pz.n, pl.pz.E, sizeof(float2));
+  while (zcols > 1 && (size_t)pl.pz.n * (zcols + 1) * sizeof(float2) * 3 > 200 * 1024) zcols >>= 1;
+  const int nthr_z = zcols * pl.pz.n / pl.pz.E;
+  const unsigned zgrid = (unsigned)((rows + zcols - 1) / zcols);
+  const size_t smz = (size_t)pl.pz.n * (zcols + 1) * sizeof(float2);
+  if (gx.tiles * 4 > L.part_doubles || (int64_t)zgrid > L.part_doubles)
+    return set_error(JLD_ERR_UNSUPPORTED, "mesh too large for the reduction buffer");
+
+  // 1 / Npixel in FP64 (model.py:386-390)
+  if (a.mask) {
+    mask_count_kernel<<<cgrid, cblock, 0, st>>>(a.mask, L.C, part);
+    inv_kernel<<<1, 1, 0, st>>>(part, (int)cgrid, npix);
+    JLD_LAUNCH_CHECK("mask_count_kernel");
+  } else {
+    set_scalar_kernel<<<1, 1, 0, st>>>(npix, 1.0 / (double)L.C);
+    JLD_LAUNCH_CHECK("set_scalar_kernel");
+  }
+
+  // ---------------- forward layers
+  for (int l = 0; l < a.nstep; ++l) {
+    const float* prm = a.params + 5 * l;
+    float* rho_l = rho + (size_t)L.C * l;
+    float2* S_l = Sbuf + (size_t)L.H * l;
+    float4* g4_l = g4 + (size_t)L.C * l;
+    if ((s = paint_unit_f32(st, Xl(l), a.N, nx, ny, nz, a.box, a.paint_method, rho_l))) return s;
+    SourcePow src{prm, fact};
+    if ((s = launch_rfft_z_src<float, SourcePow>(st, pl, rho_l, src, W[0], W[0] + nyq_off))) return s;
+    if ((s = launch_y_pass<float>(st, pl, W[0], W[0] + nyq_off, -1))) return s;
+    s = with_sched(pl.px, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(xfilt_kernel<SC>, 2 * gx.smem1);
+      if (e) return e;
+      xfilt_kernel<SC><<<(unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(pl.px, gx.sp, kt, prm, a.kind, scale,
+                                                                          W[0], S_l, W[1], W[2]);
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("xfilt_kernel");
+    s = with_sched(pl.py, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(yinv3_kernel<SC>, gy.smem1);
+      if (e) return e;
+      yinv3_kernel<SC><<<(unsigned)gy.tiles, gy.nthr, gy.smem1, st>>>(pl.py, gy.sp, kt, W[1], W[2], W[3], W[0],
+                                                                      W[4]);
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("yinv3_kernel");
+    s = with_sched(pl.pz, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(zinv3_kernel<SC>, 3 * smz);
+      if (e) return e;
+      zinv3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, W[3], W[0], W[4], nyq_off, g4_l, rows,
+                                                       zcols, ilog2i(zcols));
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("zinv3_kernel");
+    update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
+    JLD_LAUNCH_CHECK("update_kernel");
+  }
+
+  // ---------------- final map, loss and its cotangent
+  float* rho_f = rho + (size_t)L.C * a.nstep;
+  if ((s = paint_unit_f32(st, Xl(a.nstep), a.N, nx, ny, nz, a.box, a.paint_method, rho_f))) return s;
+  loss_kernel<<<cgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
+                                        a.L1, npix, rb, part);
+  JLD_LAUNCH_CHECK("loss_kernel");
+  finish_kernel<<<1, 32, 0, st>>>(part, (int)cgrid, 4, 1, a.out, 0, npix);
+  if (a.kind == 0) finish_kernel<<<1, 32, 0, st>>>(part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
+  gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
+  JLD_LAUNCH_CHECK("gather_vjp_kernel");
+
+  // ---------------- adjoint layers
+  for (int l = a.nstep - 1; l >= 0; --l) {
+    const float* prm = a.params + 5 * l;
+    float* rho_l = rho + (size_t)L.C * l;
+    float2* S_l = Sbuf + (size_t)L.H * l;
+    float4* g4_l = g4 + (size_t)L.C * l;
+    JLD_CUDA_TRY(cudaMemsetAsync(gb4, 0, sizeof(float4) * L.C, st));
+    bwd_particles_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
+    JLD_LAUNCH_CHECK("bwd_particles_kernel");
+    s = with_sched(pl.pz, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(zfwd3_kernel<SC>, 3 * smz);
+      if (e) return e;
+      zfwd3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, kt.cz, gb4, W[0], W[1], W[2], nyq_off,
+                                                       rows, zcols, ilog2i(zcols));
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("zfwd3_kernel");
+    s = with_sched(pl.py, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(yfwd_comb_kernel<SC>, 2 * gy.smem1);
+      if (e) return e;
+      yfwd_comb_kernel<SC><<<(unsigned)gy.tiles, gy.nthr, 2 * gy.smem1, st>>>(pl.py, gy.sp, kt, W[0], W[1],
+                                                                               W[2], W[3]);
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("yfwd_comb_kernel");
+    s = with_sched(pl.px, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(xbwd_kernel<SC>, 2 * gx.smem1);
+      if (e) return e;
+      xbwd_kernel<SC><<<(unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(pl.px, gx.sp, kt, prm, a.kind, a.mode,
+                                                                         scale, W[0], W[3], S_l, W[1], part);
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("xbwd_kernel");
+    // d alpha -> out[1+5l], d kh, d kl, d nu -> out[1+5l+2 .. 4]
+    finish_kernel<<<1, 32, 0, st>>>(part, (int)gx.tiles, 4, 1, a.out, 1 + 5 * l, nullptr);
+    finish_kernel<<<1, 32, 0, st>>>(part + 1, (int)gx.tiles, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
+    if ((s = launch_y_pass<float>(st, pl, W[1], W[1] + nyq_off, +1))) return s;
+    s = with_sched(pl.pz, [&](auto sc) {
+      constexpr int SC = decltype(sc)::value;
+      int e = ensure_smem(zinv_adj_kernel<SC>, smz);
+      if (e) return e;
+      zinv_adj_kernel<SC><<<zgrid, nthr_z, smz, st>>>(pl.pz, pl.twr, W[1], nyq_off, rho_l, prm, fact, rb, part,
+                                                      rows, zcols, ilog2i(zcols));
+      return 0;
+    });
+    if (s) return s;
+    JLD_LAUNCH_CHECK("zinv_adj_kernel");
+    finish_kernel<<<1, 32, 0, st>>>(part, (int)zgrid, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
+    gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
+    JLD_LAUNCH_CHECK("gather_vjp_kernel");
+    std::swap(Xb, Xb2);
+  }
+  return JLD_OK;
+}
+
+static int check_step_args(int nx, int ny, int nz, int64_t nparts, int nstep, const float* box,
+                           const char* who) {
+  if (nx < 1 || ny < 1 || nz < 2 || (nz & 1))
+    return set_error(JLD_ERR_UNSUPPORTED, "%s: mesh (%d,%d,%d) unsupported (nz must be even)", who, nx, ny, nz);
+  if (nparts < 1) return set_error(JLD_ERR_ARG, "%s: need at least one particle", who);
+  if (nstep < 1 || nstep > 64) return set_error(JLD_ERR_ARG, "%s: nstep must be in 1..64", who);
+  if (!box || !(box[0] > 0 && box[1] > 0 && box[2] > 0))
+    return set_error(JLD_ERR_ARG, "%s: box sizes must be positive", who);
+  if ((int64_t)nx * ny * nz > ((int64_t)1 << 31))
+    return set_error(JLD_ERR_UNSUPPORTED, "%s: mesh too large", who);
+  return JLD_OK;
+}
+
+}  // namespace jld
+
+using namespace jld;
+
+extern "C" {
+
+JLD_API size_t jld_ldl_workspace_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts, int32_t nstep) {
+  if (nx < 1 || ny < 1 || nz < 2 || nparts < 1 || nstep < 1) return 0;
+  return ldl_layout(nx, ny, nz, nparts, nstep).total;
+}
+
+JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float box[3]) {
+  clear_error();
+  int s = check_step_args(nx, ny, nz, 1, 1, box, "jld_ldl_prepare_f32");
+  if (s) return s;
+  Plan3<float> pl;
+  if ((s = get_plan3<float>(nx, ny, nz, true, &pl))) return s;
+  KTables kt;
+  return get_ktables(nx, ny, nz, box, true, &kt);
+}
+
+JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
+                             int32_t nz, const float box[3], int32_t nstep, int32_t kind, int32_t L1,
+                             int32_t grad_mode, int32_t paint_method, const float* params,
+                             const float* target, const float* mask, void* ws, size_t ws_bytes,
+                             double* out) {
+  clear_error();
+  const char* who = "jld_ldl_step_f32";
+  int s = check_step_args(nx, ny, nz, nparts, nstep, box, who);
+  if (s) return s;
+  if (kind != 0 && kind != 1) return set_error(JLD_ERR_ARG, "%s: kind must be 0 (sm) or 1 (dm)", who);
+  if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
+  if (grad_mode != 0 && grad_mode != 1)
+    return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
+  if (paint_method != 0 && paint_method != 1)
+    return set_error(JLD_ERR_ARG, "%s: paint_method must be 0 or 1", who);
+  if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
+  size_t need = ldl_layout(nx, ny, nz, nparts, nstep).total;
+  if (!ws || ws_bytes < need)
+    return set_error(JLD_ERR_WORKSPACE, "%s: workspace of %zu bytes needed, got %zu", who, need,
+                     ws ? ws_bytes : (size_t)0);
+  StepArgs a;
+  a.st = reinterpret_cast<cudaStream_t>(stream);
+  a.pos0 = pos; a.N = nparts;
+  a.nx = nx; a.ny = ny; a.nz = nz;
+  for (int i = 0; i < 3; ++i) a.box[i] = box[i];
+  a.nstep = nstep; a.kind = kind; a.L1 = L1; a.mode = grad_mode; a.paint_method = paint_method;
+  a.params = params; a.target = target; a.mask = mask;
+  a.ws = (char*)ws; a.out = out;
+  return ldl_step(a);
+}
+
+JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                                  int32_t nstep, int32_t layer, const float** out) {
+  clear_error();
+  if (!ws || !out || layer < 1 || layer > nstep)
+    return set_error(JLD_ERR_ARG, "jld_ldl_positions_f32: bad arguments");
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  *out = (const float*)((const char*)ws + L.off_pos) + (size_t)3 * nparts * (layer - 1);
+  return JLD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+"""Fused LDL forward + adjoint step (libjld's jld_ldl_step_f32) with CUDA-graph
+capture.
+
+One call evaluates the loss of model.py (kinds "sm" and "dm") and its
+gradient with respect to every parameter, the way
+JERALDModel.loss_and_grad does through the primitives, but with the
+elementwise source, filter and gradient kernels fused into the FFT passes,
+a float4 force mesh for the readout, float4 vector atomics for the adjoint
+paint and FP64 reductions for the loss and the parameter gradients.
+
+    step = FusedLDL(nmesh=512, box=1000.0, nparts=N, nstep=2, kind="sm")
+    loss, grad = step(pos, params, target)          # eager
+    step.capture(pos, target)                        # CUDA graph on static inputs
+    loss, grad = step.replay(params)                 # one graph launch per step
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_KINDS = {"sm": 0, "dm": 1}
+_MODES = {"reference": 0, "true": 1}
+_PAINT = {"atomic": 0, "warp": 1}
+
+
+class FusedLDL:
+    def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
+                 grad_mode: str = "reference", paint_method: str = "atomic", device="cuda"):
+        nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
+        self.nmesh = tuple(int(v) for v in nm)
+        self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
+        if kind not in _KINDS:
+            raise ValueError("kind must be 'sm' or 'dm' for the fused step (use JERALDModel for 'HI')")
+        self.kind = kind
+        self.L1 = (kind != "dm") if L1 is None else bool(L1)
+        self.grad_mode = grad_mode
+        self.paint_method = paint_method
+        self.nparts = int(nparts)
+        self.nstep = int(nstep)
+        self.nparams = 5 * self.nstep + (3 if kind == "sm" else 0)
+        self.device = torch.device(device)
+        lib = _lib.load()
+        nbytes = lib.jld_ldl_workspace_f32(*self.nmesh, self.nparts, self.nstep)
+        if nbytes == 0:
+            raise ValueError("invalid fused-step geometry")
+        self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
+        self.out = torch.zeros(1 + self.nparams, dtype=torch.float64, device=self.device)
+        self.params = torch.zeros(self.nparams, dtype=torch.float32, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.call("jld_ldl_prepare_f32", *self.nmesh, self.box.ctypes.data_as(ct.c_void_p))
+        self.graph = None
+        self._static = None
+
+    @property
+    def workspace_bytes(self) -> int:
+        return self.ws.numel()
+
+    def _launch(self, pos: torch.Tensor, target: torch.Tensor, mask):
+        if pos.dtype != torch.float32 or not pos.is_contiguous() or pos.shape != (self.nparts, 3):
+            raise ValueError("pos must be a contiguous float32 (nparts, 3) CUDA tensor")
+        if target.dtype != torch.float32 or not target.is_contiguous() or target.numel() != np.prod(self.nmesh):
+            raise ValueError("target must be a contiguous float32 mesh")
+        if mask is not None and (mask.dtype != torch.float32 or not mask.is_contiguous()):
+            raise ValueError("mask must be a contiguous float32 mesh")
+        st = ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        _lib.call("jld_ldl_step_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
+                  self.box.ctypes.data_as(ct.c_void_p), self.nstep, _KINDS[self.kind], int(self.L1),
+                  _MODES[self.grad_mode], _PAINT[self.paint_method], ct.c_void_p(self.params.data_ptr()),
+                  ct.c_void_p(target.data_ptr()), ct.c_void_p(mask.data_ptr()) if mask is not None else None,
+                  ct.c_void_p(self.ws.data_ptr()), self.ws.numel(), ct.c_void_p(self.out.data_ptr()))
+
+    def _set_params(self, params):
+        p = torch.as_tensor(params, dtype=torch.float32).reshape(-1)
+        if p.numel() != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {p.numel()}")
+        self.params.copy_(p.to(self.device), non_blocking=True)
+
+    def __call__(self, pos, params, target, mask=None):
+        """Eager step; returns (loss, grad) as float64 device tensors."""
+        self._set_params(params)
+        self._launch(pos, target, mask)
+        return self.out[0], self.out[1:]
+
+    def capture(self, pos, target, mask=None):
+        """Captures the step on static inputs (they must stay alive and in place)."""
+        self._static = (pos, target, mask)
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self._launch(pos, target, mask)  # builds plans, tables and kernel attributes
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._launch(pos, target, mask)
+        return self.graph
+
+    def replay(self, params=None):
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        if params is not None:
+            self._set_params(params)
+        self.graph.replay()
+        return self.out[0], self.out[1:]
+
+    def positions(self, layer: int) -> torch.Tensor:
+        """(nparts, 3) view of the positions after `layer` layers of the last step."""
+        ptr = ct.c_void_p()
+        _lib.call("jld_ldl_positions_f32", ct.c_void_p(self.ws.data_ptr()), *self.nmesh, self.nparts,
+                  self.nstep, int(layer), ct.byref(ptr))
+        off = ptr.value - self.ws.data_ptr()
+        return self.ws[off: off + 12 * self.nparts].view(torch.float32).view(self.nparts, 3)

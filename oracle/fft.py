@@ -15,12 +15,26 @@ from __future__ import annotations
 import numpy as np
 
 
+_WORKERS = {"n": 1}
+
+
+def set_workers(n: int) -> None:
+    """Use scipy.fft (pocketfft) with n threads instead of numpy (1 thread)."""
+    _WORKERS["n"] = max(1, int(n))
+
+
 def pfft(x: np.ndarray) -> np.ndarray:
+    if _WORKERS["n"] > 1:
+        import scipy.fft
+        return scipy.fft.rfftn(x, workers=_WORKERS["n"])
     return np.fft.rfftn(x)
 
 
 def pifft(y: np.ndarray, shape) -> np.ndarray:
     shape = tuple(int(s) for s in shape)
+    if _WORKERS["n"] > 1:
+        import scipy.fft
+        return scipy.fft.irfftn(y, s=shape, axes=(0, 1, 2), workers=_WORKERS["n"]) * float(np.prod(shape))
     return np.fft.irfftn(y, s=shape, axes=(0, 1, 2)) * float(np.prod(shape))
 
 

@@ -1,0 +1,124 @@
+"""GPU parity of the fused LDL step (C ABI jld_ldl_step_f32 via FusedLDL)
+against the FP64 oracle, the plain primitive path, and its own CUDA graph.
+
+Tolerances (FP32 bulk, FP64 reductions): loss within 1e-5 relative, each
+gradient component within 1e-3 relative at these small meshes (FD-level
+quantities; components below 1e-6 of the largest are compared absolutely).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from oracle.ldl import LDLOracle  # noqa: E402
+
+
+def _case(n, box, kind, L1, seed, rms=0.5, mask=False, nstep=2):
+    from jerald_gb300 import synth
+    X = synth.zeldovich(n, box, rms, seed=seed, dtype=np.float32).astype(np.float64)
+    p = synth.default_params(nstep)
+    if kind == "dm":
+        p = p[:5 * nstep]
+    o = LDLOracle((n, n, n), box, kind=kind, L1=L1)
+    o.forward(p, X, np.ones((n, n, n)), nstep)
+    tgt = (o.cache["F"] * synth.lognormal_noise((n, n, n), 0.1, seed + 1)).astype(np.float32)
+    m = np.random.default_rng(seed + 2).integers(0, 2, (n, n, n)).astype(np.float32) if mask else None
+    return X, p, tgt, o, m
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-6 * np.abs(b).max())
+
+
+def _fused(n, box, N, kind, L1, mode, nstep=2, paint="atomic"):
+    from jerald_gb300.ldl import FusedLDL
+    return FusedLDL(n, box, N, nstep=nstep, kind=kind, L1=L1, grad_mode=mode, paint_method=paint)
+
+
+@pytest.mark.parametrize("kind,L1,mask", [("sm", True, False), ("sm", False, True), ("dm", False, False)])
+@pytest.mark.parametrize("mode", ["reference", "true"])
+def test_fused_matches_fp64_oracle(kind, L1, mask, mode):
+    n, box = 32, 100.0
+    X, p, tgt, o, m = _case(n, box, kind, L1, 21, mask=mask)
+    loss_o, g_o = o.loss_and_grad(p, X, tgt.astype(np.float64), 2,
+                                  mask=None if m is None else m.astype(np.float64), mode=mode)
+    f = _fused(n, box, len(X), kind, L1, mode)
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    t = torch.from_numpy(tgt).cuda()
+    mk = torch.from_numpy(m).cuda() if m is not None else None
+    loss, g = f(pos, p, t, mk)
+    torch.cuda.synchronize()
+    assert abs(float(loss) - loss_o) <= 1e-5 * abs(loss_o)
+    assert _rel(g.cpu().numpy(), g_o).max() < 1e-3
+
+
+def test_fused_positions_match_oracle_layers():
+    n, box = 32, 100.0
+    X, p, tgt, o, _ = _case(n, box, "sm", True, 5)
+    f = _fused(n, box, len(X), "sm", True, "reference")
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    f(pos, p, torch.from_numpy(tgt).cuda())
+    torch.cuda.synchronize()
+    # X_1 of the oracle: rerun its first layer
+    X1, _ = o.layer_forward(X, p[:5], float(n ** 3) / len(X))
+    got = f.positions(1).cpu().numpy().astype(np.float64)
+    disp = np.abs(X1 - X).max()
+    assert np.abs(got - X1).max() < 1e-4 * max(disp, 1.0) + 2e-5 * box
+
+
+def test_fused_matches_plain_primitives():
+    from jerald_gb300.model import JERALDModel
+    from jerald_gb300.pmesh import PMesh
+    n, box = 64, 200.0
+    X, p, tgt, o, _ = _case(n, box, "sm", True, 9, rms=1.0)
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    t = torch.from_numpy(tgt).cuda()
+    pm = PMesh(n, box, dtype=torch.float32)
+    model = JERALDModel(pos, t, pm, Nstep=2, kind="sm")
+    lp, gp = model.loss_and_grad(torch.from_numpy(p.astype(np.float32)))
+    f = _fused(n, box, len(X), "sm", True, "reference")
+    lf, gf = f(pos, p, t)
+    torch.cuda.synchronize()
+    assert abs(float(lf) - float(lp)) <= 2e-5 * abs(float(lp))
+    assert _rel(gf.cpu().numpy(), gp.cpu().numpy()).max() < 5e-3
+
+
+@pytest.mark.parametrize("paint", ["atomic", "warp"])
+def test_fused_graph_replay_matches_eager(paint):
+    n, box = 32, 100.0
+    X, p, tgt, o, _ = _case(n, box, "sm", True, 13)
+    f = _fused(n, box, len(X), "sm", True, "reference", paint=paint)
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    t = torch.from_numpy(tgt).cuda()
+    l0, g0 = [v.clone() for v in f(pos, p, t)]
+    f.capture(pos, t)
+    l1, g1 = [v.clone() for v in f.replay(p)]
+    torch.cuda.synchronize()
+    assert abs(float(l1) - float(l0)) <= 1e-6 * abs(float(l0))
+    assert _rel(g1.cpu().numpy(), g0.cpu().numpy()).max() < 1e-4
+    # new parameters through the same graph
+    p2 = p * 1.1
+    l2, g2 = [v.clone() for v in f.replay(p2)]
+    l3, g3 = [v.clone() for v in f(pos, p2, t)]
+    torch.cuda.synchronize()
+    assert abs(float(l2) - float(l3)) <= 1e-6 * abs(float(l3))
+    assert abs(float(l2) - float(l0)) > 1e-6 * abs(float(l0))
+
+
+def test_fused_rejects_bad_arguments():
+    from jerald_gb300 import _lib
+    from jerald_gb300.ldl import FusedLDL
+    with pytest.raises(ValueError):
+        FusedLDL(16, 10.0, 100, kind="HI")
+    f = FusedLDL(16, 10.0, 4096, kind="sm")
+    pos = torch.zeros((4096, 3), device="cuda")
+    with pytest.raises(ValueError):
+        f(pos, np.zeros(3), torch.zeros((16, 16, 16), device="cuda"))
+    f.grad_mode = "bogus"
+    with pytest.raises(KeyError):
+        f(pos, np.zeros(13), torch.zeros((16, 16, 16), device="cuda"))
+    with pytest.raises(_lib.JLDError):
+        FusedLDL((16, 16, 15), 10.0, 100)

@@ -32,8 +32,22 @@ def _p(t):
     return ct.c_void_p(t.data_ptr())
 
 
+_LIVE = []
+
+
+@pytest.fixture(autouse=True)
+def _release_inputs():
+    yield
+    torch.cuda.synchronize()
+    _LIVE.clear()
+
+
 def _cuda(a):
-    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    # Device copies stay referenced until the test ends: a raw pointer handed
+    # to the C ABI does not keep the tensor (and its allocator block) alive.
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    _LIVE.append(t)
+    return t
 
 
 def _box(box, dt):
