@@ -232,6 +232,67 @@ def run_reference(args):
     return 0
 
 
+def run_profile(args):
+    """Eager fused steps only: the kernels ncu sees are the step's own."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    dev = torch.device("cuda", 0)
+    n = args.n
+    params = synth.default_params(2)
+    pos, box = make_workload(n, dev, seed=0)
+    target = torch.ones((n, n, n), device=dev)
+    step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, paint_method=args.paint, device=dev)
+    for _ in range(args.warmup + args.steps):
+        step(pos, params, target)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": True, "n": n, "nparts": int(pos.shape[0]), "loss": float(step.out[0]),
+                      "launches_per_step": count_launches(2, "sm", False)}))
+    return 0
+
+
+def run_precision(args):
+    """Fused FP32 step vs the FP64 primitive pipeline (plain JERALDModel in
+    float64 on the same positions and target): loss and gradient errors."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    from jerald_gb300.model import JERALDModel
+    from jerald_gb300.pmesh import PMesh
+    dev = torch.device("cuda", 0)
+    n = args.n
+    params = synth.default_params(2)
+    pos, box = make_workload(n, dev, seed=0)
+    target = make_target(pos, n, box, params, dev)
+    res = {"precision": True, "n": n, "nparts": int(pos.shape[0])}
+    for mode in ("reference", "true"):
+        step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, grad_mode=mode, device=dev)
+        l32, g32 = step(pos, params, target)
+        l32, g32 = float(l32), g32.cpu().numpy()
+        del step
+        torch.cuda.empty_cache()
+        from jerald_gb300 import jaxpops_bind as jpo
+        jpo.set_fft_adjoint(mode)
+        pm = PMesh(n, box, device=dev, dtype=torch.float64)
+        model = JERALDModel(pos.double(), target.double(), pm, Nstep=2, kind="sm")
+        l64, g64 = model.loss_and_grad(torch.as_tensor(params, dtype=torch.float64))
+        jpo.set_fft_adjoint("reference")
+        l64, g64 = float(l64), g64.cpu().numpy()
+        del model, pm
+        torch.cuda.empty_cache()
+        rel = np.abs(g32 - g64) / np.abs(g64)
+        res[mode] = {"loss_f32": l32, "loss_f64": l64, "loss_rel_err": abs(l32 - l64) / abs(l64),
+                     "grad_rel_err_max": float(rel.max()), "grad_rel_err": rel.tolist(),
+                     "grad_norm_rel_err": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+                     "grad_f64": g64.tolist()}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -241,11 +302,20 @@ def main():
     ap.add_argument("--n", type=int, default=512, help="mesh size per axis (workload scale)")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain primitive path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true",
+                    help="run only eager fused steps (warmup + steps) on the workload, for ncu")
+    ap.add_argument("--precision", action="store_true",
+                    help="compare the fused FP32 step with the FP64 primitive pipeline on the workload")
+    ap.add_argument("--paint", default="atomic", choices=["atomic", "warp"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
+    if args.precision:
+        return run_precision(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
