@@ -209,6 +209,20 @@ JLD_API int jld_pifft_c_f32(jld_stream_t stream, const void* in_c, int32_t nx, i
 JLD_API int jld_pifft_c_f64(jld_stream_t stream, const void* in_c, int32_t nx, int32_t ny,
                     int32_t nz, double* out, void* ws, size_t ws_bytes);
 
+/* Allocation-free variant of jld_pfft_c_f32 (no counterpart in the       */
+/* reference).  For callers that cannot allocate device memory (a host     */
+/* framework that owns all allocations, or a phase where allocating is not */
+/* allowed): it takes no workspace and allocates nothing, keeping its      */
+/* scratch and twiddle tables in fixed device arrays inside libjld (72 MiB */
+/* of scratch, held by every GPU that loads the library until exit).       */
+/* Limits: nx * ny * (nz/2 + 1) * 8 bytes <= 72 MiB (256^3 fits) and each */
+/* size <= 4096; larger meshes return JLD_ERR_WORKSPACE / UNSUPPORTED.     */
+/* The first call on a device resolves the arrays' addresses (make it      */
+/* before any stream capture).  All calls share the arrays: calls that     */
+/* overlap on the GPU race.                                                */
+JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_t nx,
+                                  int32_t ny, int32_t nz, void* out_c);
+
 /* ------------------------------------------------------------------ */
 /* Fused LDL step: forward of `nstep` displacement layers, final map and  */
 /* loss, and the adjoint, in one stream-ordered call.  It computes what   */

@@ -55,6 +55,7 @@ _SIGS = {
     "jld_pifft_f64": [_c_void_p, _c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
     "jld_pifft_c_f32": [_c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
     "jld_pifft_c_f64": [_c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p, _c_void_p, _size],
+    "jld_pfft_c_static_f32": [_c_void_p, _c_void_p, _i32, _i32, _i32, _c_void_p],
     "jld_ldl_prepare_f32": [_i32, _i32, _i32, _c_void_p],
     "jld_ldl_step_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32, _i32,
                          _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],

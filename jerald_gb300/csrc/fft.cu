@@ -233,6 +233,114 @@ static int irfft3(cudaStream_t st, const cplx_t<T>* in_c, const T* in_re, const 
   return launch_irfft_z<T>(st, pl, main, nyq, out);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free r2c (jld_pfft_c_static_f32).
+//
+// For callers that cannot allocate device memory themselves -- code running
+// inside a host framework that owns every allocation, or code running where
+// allocation is forbidden (for example between the setup and the launch of a
+// captured sequence) -- this variant keeps its scratch and its twiddle tables
+// in file-scope device arrays instead of a caller workspace and the plan
+// cache.  Limits: the internal half spectrum (nx * ny * (nz/2 + 1) complex
+// floats) must fit in kStaticScratchBytes = 72 MiB (256^3 fits), and each of
+// nx, ny, nz must be at most 4096.  The arrays are part of the library image,
+// so every GPU that loads libjld holds them until the process exits.
+//
+// Host code must not pass the arrays' names to a kernel: on the host they are
+// stand-ins, not device addresses.  The first call on each device resolves
+// their device addresses with cudaGetSymbolAddress (with that device
+// current); make that first call before any stream capture.  Every call
+// shares the arrays and overwrites them (the scratch needs no clearing: each
+// pass writes all of it before it is read), so calls that overlap on the GPU
+// -- on two streams, or on one device from two threads -- race.
+static constexpr size_t kStaticScratchBytes = (size_t)72 << 20;
+static constexpr int kStaticMaxLen = 4096;
+static constexpr int kStaticTwLen = 2 * kStaticMaxLen + kStaticMaxLen / 2 + kStaticMaxLen / 2 + 1;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+static __device__ __align__(256) float2 g_static_tw[kStaticTwLen];
+
+struct StaticDev {
+  bool ready = false;
+  void* scratch = nullptr;
+  float2* tw = nullptr;
+};
+static std::mutex g_static_mu;
+static StaticDev g_static_dev[64];
+
+// Resolves the device addresses of the file-scope arrays once per device.
+static int static_setup(StaticDev* out) {
+  int dev = 0;
+  JLD_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(JLD_ERR_UNSUPPORTED, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  StaticDev& s = g_static_dev[dev];
+  if (!s.ready) {
+    JLD_CUDA_TRY(cudaGetSymbolAddress(&s.scratch, g_static_scratch));
+    JLD_CUDA_TRY(cudaGetSymbolAddress((void**)&s.tw, g_static_tw));
+    s.ready = true;
+  }
+  *out = s;
+  return JLD_OK;
+}
+
+// tw[m] = exp(-2 pi i (m mod n) / n) in FP64, rounded to float.
+__global__ void static_twiddles_kernel(float2* tw, int n, int count) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < count; m += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)(m % n) / (double)n, &s, &c);
+    tw[m] = make_float2((float)c, (float)(-s));
+  }
+}
+
+static int pfft_static_impl(cudaStream_t st, const float* data, int nx, int ny, int nz, float2* out_c) {
+  const char* who = "jld_pfft_c_static_f32";
+  if (!data || !out_c) return set_error(JLD_ERR_ARG, "%s: NULL data or output", who);
+  if (nx < 1 || ny < 1 || nz < 2) return set_error(JLD_ERR_ARG, "%s: mesh sizes must be positive (nz >= 2)", who);
+  if (nz & 1) return set_error(JLD_ERR_UNSUPPORTED, "%s: nz must be even", who);
+  if (nx > kStaticMaxLen || ny > kStaticMaxLen || nz > kStaticMaxLen)
+    return set_error(JLD_ERR_UNSUPPORTED, "%s: each mesh size must be at most %d", who, kStaticMaxLen);
+  const int h = nz / 2;
+  const size_t need = (size_t)nx * ny * (h + 1) * sizeof(float2);
+  if (need > kStaticScratchBytes)
+    return set_error(JLD_ERR_WORKSPACE,
+                     "%s: mesh (%d,%d,%d) needs %zu bytes of scratch, more than the fixed %zu bytes", who, nx,
+                     ny, nz, need, kStaticScratchBytes);
+  Plan3<float> pl;
+  pl.nx = nx; pl.ny = ny; pl.nz = nz; pl.h = h;
+  LinePlan<float>* lp[3] = {&pl.px, &pl.py, &pl.pz};
+  const int lens[3] = {nx, ny, h};
+  for (int a = 0; a < 3; ++a) {
+    lp[a]->n = lens[a];
+    if (!make_line_schedule(lens[a], &lp[a]->E, &lp[a]->nst, lp[a]->radix))
+      return set_error(JLD_ERR_UNSUPPORTED, "%s: length %d does not factor into 2, 3 and 5", who, lens[a]);
+    for (int s = lp[a]->nst; s < kMaxStages; ++s) lp[a]->radix[s] = 0;
+  }
+  StaticDev sd;
+  int s = static_setup(&sd);
+  if (s) return s;
+  float2* tw = sd.tw;
+  pl.px.tw = tw;
+  pl.py.tw = tw + nx;
+  pl.pz.tw = tw + nx + ny;
+  pl.twr = tw + nx + ny + h;
+  const int tl[4] = {nx, ny, h, nz}, tc[4] = {nx, ny, h, h + 1};
+  size_t off = 0;
+  for (int i = 0; i < 4; ++i) {
+    static_twiddles_kernel<<<(tc[i] + 255) / 256, 256, 0, st>>>(tw + off, tl[i], tc[i]);
+    off += tc[i];
+  }
+  JLD_LAUNCH_CHECK("static_twiddles_kernel");
+  float2* main = (float2*)sd.scratch;
+  float2* nyq = main + (size_t)nx * ny * h;
+  if ((s = launch_rfft_z<float>(st, pl, data, nullptr, main, nyq))) return s;
+  if ((s = launch_y_pass<float>(st, pl, main, nyq, -1))) return s;
+  LineJob<float> jm = job_x_internal<float>(pl, main, false);
+  LineJob<float> jn = job_x_internal<float>(pl, nyq, true);
+  set_job_out_ref<float>(jm, pl, false, out_c, nullptr, nullptr);
+  set_job_out_ref<float>(jn, pl, true, out_c, nullptr, nullptr);
+  return launch_line_pass<float>(st, pl.px, jm, jn, -1);
+}
+
 }  // namespace jld
 
 using namespace jld;
@@ -308,6 +416,12 @@ int jld_pifft_c_f64(jld_stream_t s, const void* in, int32_t nx, int32_t ny, int3
   clear_error();
   return irfft3<double>(ST(s), (const double2*)in, nullptr, nullptr, nx, ny, nz, out, ws, wsb,
                         "jld_pifft_c_f64");
+}
+
+int jld_pfft_c_static_f32(jld_stream_t s, const float* data, int32_t nx, int32_t ny, int32_t nz,
+                          void* out) {
+  clear_error();
+  return pfft_static_impl(ST(s), data, nx, ny, nz, (float2*)out);
 }
 
 }  // extern "C"
