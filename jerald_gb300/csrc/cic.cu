@@ -243,8 +243,9 @@ static int check_common(const void* pos, int64_t nparts, const void* out,
   if (!out) return set_error(JLD_ERR_ARG, "%s: output is NULL", who);
   if (nx <= 0 || ny <= 0 || nz <= 0)
     return set_error(JLD_ERR_ARG, "%s: mesh sizes must be positive", who);
-  if (nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30))
-    return set_error(JLD_ERR_ARG, "%s: mesh size too large", who);
+  if (nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30) ||
+      (double)nx * (double)ny * (double)nz >= 4294967296.0)
+    return set_error(JLD_ERR_UNSUPPORTED, "%s: mesh too large (needs fewer than 2^32 cells)", who);
   return JLD_OK;
 }
 

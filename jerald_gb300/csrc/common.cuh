@@ -70,10 +70,24 @@ inline Grid3 make_grid(int64_t nx, int64_t ny, int64_t nz) {
 // Box-to-mesh prelude of jaxpops_bind.py:163-164 in the working dtype:
 // r = x mod L with jnp.remainder semantics (C fmod, plus L when the signs of
 // r and L differ and r is nonzero), then r / (L/N) with IEEE division.
+// The common cases take exact shortcuts with identical results (box > 0):
+//   0 <= x < L    fmod(x, L) = x
+//   L <= x < 2L   fmod(x, L) = x - L, exact by Sterbenz' lemma
+//   -L < x < 0    fmod(x, L) = x; the signs differ, so r = x + L (rounded)
+// anything else (|x| >= 2L, x = -L, NaN) goes through fmod.
 template <typename T>
 __device__ __forceinline__ T box_to_mesh(T x, T box, T cell) {
-  T r = fmod(x, box);
-  if (r != T(0) && ((r < T(0)) != (box < T(0)))) r = r + box;
+  T r;
+  if (x >= T(0) && x < box) {
+    r = x;
+  } else if (x >= box && x < T(2) * box) {
+    r = x - box;
+  } else if (x < T(0) && x > -box) {
+    r = x + box;
+  } else {
+    r = fmod(x, box);
+    if (r != T(0) && ((r < T(0)) != (box < T(0)))) r = r + box;
+  }
   return r / cell;
 }
 
@@ -94,26 +108,38 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 // (t = 1-d and d in the reference), `ok_lo[a]` / `ok_hi[a]` the validity
 // flags (inx.. / inpx..) and `cell_lo[a]` / `cell_hi[a]` the wrapped
 // indices.  At world size one the rank edges are [0, N) on every axis.
+// Offsets are 32-bit: the CIC entry points require Nx*Ny*Nz < 2^32.
 template <typename T>
 struct Corners {
-  int c_lo[3], c_hi[3];
-  bool ok_lo[3], ok_hi[3];
-  T d[3];  // fractional offsets p - int(p)
+  uint32_t o[3][2];  // per-axis offset (index * stride) of the lower / upper corner
+  bool ok[3][2];     // per-axis validity flags (inx / inpx ...)
+  T d[3];            // fractional offsets p - int(p)
 };
 
 template <typename T>
 __device__ __forceinline__ void cic_corners(const T p[3], const Grid3& g,
                                             Corners<T>& c) {
   const int n[3] = {g.nx, g.ny, g.nz};
+  const uint32_t st[3] = {(uint32_t)g.sx, (uint32_t)g.sy, 1u};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     int i = (int)p[a];                 // C++ int(): truncation toward zero
     c.d[a] = sub_rn(p[a], (T)i);
-    int ip1 = (i + 1) % n[a];          // C remainder semantics
-    c.ok_lo[a] = (unsigned)i < (unsigned)n[a];
-    c.ok_hi[a] = (unsigned)ip1 < (unsigned)n[a];
-    c.c_lo[a] = abs(i % n[a]);
-    c.c_hi[a] = abs(ip1 % n[a]);
+    int lo, hi;
+    if ((unsigned)i < (unsigned)n[a]) {  // in range: i % n = i, (i+1) % n = i+1 or 0
+      lo = i;
+      hi = (i + 1 == n[a]) ? 0 : i + 1;
+      c.ok[a][0] = true;
+      c.ok[a][1] = true;
+    } else {                             // C remainder semantics of the reference
+      int ip1 = (i + 1) % n[a];
+      c.ok[a][0] = false;
+      c.ok[a][1] = (unsigned)ip1 < (unsigned)n[a];
+      lo = abs(i % n[a]);
+      hi = abs(ip1 % n[a]);
+    }
+    c.o[a][0] = (uint32_t)lo * st[a];
+    c.o[a][1] = (uint32_t)hi * st[a];
   }
 }
 
@@ -127,19 +153,14 @@ __device__ __forceinline__ int corner_axis_bits(int q) {
 }
 
 template <typename T>
-__device__ __forceinline__ int64_t corner_offset(const Corners<T>& c, int bits,
-                                                 const Grid3& g) {
-  int ix = (bits & 1) ? c.c_hi[0] : c.c_lo[0];
-  int iy = (bits & 2) ? c.c_hi[1] : c.c_lo[1];
-  int iz = (bits & 4) ? c.c_hi[2] : c.c_lo[2];
-  return (int64_t)ix * g.sx + (int64_t)iy * g.sy + iz;
+__device__ __forceinline__ uint32_t corner_offset(const Corners<T>& c, int bits,
+                                                  const Grid3&) {
+  return c.o[0][bits & 1] + c.o[1][(bits >> 1) & 1] + c.o[2][(bits >> 2) & 1];
 }
 
 template <typename T>
 __device__ __forceinline__ bool corner_ok(const Corners<T>& c, int bits) {
-  return ((bits & 1) ? c.ok_hi[0] : c.ok_lo[0]) &&
-         ((bits & 2) ? c.ok_hi[1] : c.ok_lo[1]) &&
-         ((bits & 4) ? c.ok_hi[2] : c.ok_lo[2]);
+  return c.ok[0][bits & 1] && c.ok[1][(bits >> 1) & 1] && c.ok[2][(bits >> 2) & 1];
 }
 
 }  // namespace jld

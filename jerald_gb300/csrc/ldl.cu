@@ -80,6 +80,12 @@ static SpecGeom spec_geom(const LinePlan<float>& lp, int nx, int ny, int h, int 
   return g;
 }
 
+// Sums per-block partial slots into out[out_off + j], j < nvals.
+static void launch_finish(cudaStream_t st, const double* part, int nblocks, int stride, int nvals,
+                          double* out, int out_off, const double* scale) {
+  finish_kernel<<<nvals, 256, 0, st>>>(part, nblocks, stride, nvals, out, out_off, scale, 0);
+}
+
 static int ldl_step(const StepArgs& a) {
   const int nx = a.nx, ny = a.ny, nz = a.nz, h = nz / 2;
   const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep);
@@ -136,8 +142,9 @@ static int ldl_step(const StepArgs& a) {
   // 1 / Npixel in FP64 (model.py:386-390)
   if (a.mask) {
     mask_count_kernel<<<cgrid, cblock, 0, st>>>(a.mask, L.C, part);
-    inv_kernel<<<1, 1, 0, st>>>(part, (int)cgrid, npix);
     JLD_LAUNCH_CHECK("mask_count_kernel");
+    finish_kernel<<<1, 256, 0, st>>>(part, (int)cgrid, 1, 1, npix, 0, nullptr, 1);
+    JLD_LAUNCH_CHECK("finish_kernel");
   } else {
     set_scalar_kernel<<<1, 1, 0, st>>>(npix, 1.0 / (double)L.C);
     JLD_LAUNCH_CHECK("set_scalar_kernel");
@@ -193,8 +200,8 @@ static int ldl_step(const StepArgs& a) {
   loss_kernel<<<cgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
                                         a.L1, npix, rb, part);
   JLD_LAUNCH_CHECK("loss_kernel");
-  finish_kernel<<<1, 32, 0, st>>>(part, (int)cgrid, 4, 1, a.out, 0, npix);
-  if (a.kind == 0) finish_kernel<<<1, 32, 0, st>>>(part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
+  launch_finish(st, part, (int)cgrid, 4, 1, a.out, 0, npix);
+  if (a.kind == 0) launch_finish(st, part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
   gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
   JLD_LAUNCH_CHECK("gather_vjp_kernel");
 
@@ -238,8 +245,8 @@ static int ldl_step(const StepArgs& a) {
     if (s) return s;
     JLD_LAUNCH_CHECK("xbwd_kernel");
     // d alpha -> out[1+5l], d kh, d kl, d nu -> out[1+5l+2 .. 4]
-    finish_kernel<<<1, 32, 0, st>>>(part, (int)gx.tiles, 4, 1, a.out, 1 + 5 * l, nullptr);
-    finish_kernel<<<1, 32, 0, st>>>(part + 1, (int)gx.tiles, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
+    launch_finish(st, part, (int)gx.tiles, 4, 1, a.out, 1 + 5 * l, nullptr);
+    launch_finish(st, part + 1, (int)gx.tiles, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
     if ((s = launch_y_pass<float>(st, pl, W[1], W[1] + nyq_off, +1))) return s;
     s = with_sched(pl.pz, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
@@ -251,7 +258,7 @@ static int ldl_step(const StepArgs& a) {
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv_adj_kernel");
-    finish_kernel<<<1, 32, 0, st>>>(part, (int)zgrid, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
+    launch_finish(st, part, (int)zgrid, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
     gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
     JLD_LAUNCH_CHECK("gather_vjp_kernel");
     std::swap(Xb, Xb2);

@@ -500,6 +500,29 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* __re
   }
 }
 
+// Compensated (Kahan) FP32 running sum for per-thread partials (a thread
+// covers tens of elements); the cross-thread and cross-block sums are FP64.
+// FP64 arithmetic per element would be slow on this part.
+struct KahanF {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = __fsub_rn(x, c);
+    float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_kahan(const KahanF (&k)[NV], double* __restrict__ out,
+                                                   int slot_stride) {
+  double v[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = k[i].value();
+  block_reduce_store<NV>(v, out, slot_stride);
+}
+
 // Final map, loss and its cotangent (model.py:311-403).  Partials per block:
 // [loss, d mu, d w, d b].  rb = fact * d loss / d rho.
 __global__ void __launch_bounds__(256)
@@ -511,7 +534,7 @@ loss_kernel(const float* __restrict__ rho_paint, const float* __restrict__ targe
   const float w = kind == 0 ? __ldg(fparams + 1) : 0.f;
   const float b = kind == 0 ? __ldg(fparams + 2) : 0.f;
   const float inpx = (float)(*inv_npix);
-  double acc[4] = {0, 0, 0, 0};
+  KahanF acc[4];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < C;
        e += (int64_t)gridDim.x * blockDim.x) {
     float rho = __fmul_rn(__ldg(rho_paint + e), fact);
@@ -527,22 +550,23 @@ loss_kernel(const float* __restrict__ rho_paint, const float* __restrict__ targe
     }
     float diff = F - __ldg(target + e);
     float ad = fabsf(diff) * m;
-    acc[0] += L1 ? (double)ad : (double)ad * (double)ad;
+    acc[0].add(L1 ? ad : ad * ad);
     float sg = diff >= 0.f ? 1.f : -1.f;
     float ctF = (L1 ? sg * m : 2.f * fabsf(diff) * m * m * sg) * inpx;
     float r;
     if (kind == 0) {
       float ctu = u > 1e-12f ? ctF : 0.f;
-      acc[1] += (double)ctu * w * pw * logf(base);
-      acc[2] += (double)ctu * pw;
-      acc[3] += (double)ctu;
-      r = ctu * w * mu * powf(base, mu - 1.f) * fact;
+      acc[1].add(ctu * w * pw * logf(base));
+      acc[2].add(ctu * pw);
+      acc[3].add(ctu);
+      // base^(mu-1) = pw / base (base > 0)
+      r = ctu * w * mu * (pw / base) * fact;
     } else {
       r = ctF * fact;
     }
     rb[e] = r;
   }
-  block_reduce_store<4>(acc, partials, 4);
+  block_reduce_kahan<4>(acc, partials, 4);
 }
 
 // Adjoint z pass: ct_s = c2r(V); per element the source adjoint.
@@ -568,7 +592,7 @@ zinv_adj_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2
   __syncthreads();
   fft_tile<float, SCHED>(sm, ld, pl, cshift, +1, tid, nthr);
   const float gamma = __ldg(params + 1);
-  double acc[1] = {0};
+  KahanF acc[1];
   for (int f = tid; f < cols * h; f += nthr) {
     int c = f / h, m = f - c * h;
     int64_t row = row0 + c;
@@ -582,12 +606,13 @@ zinv_adj_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2
         float base = __fadd_rn(rho, 1e-8f);
         float lb = logf(base);
         float s = powf(base, gamma);
-        acc[0] += (double)cts * s * lb;
-        rb[e + q] = cts * gamma * powf(base, gamma - 1.f) * fact;
+        acc[0].add(cts * s * lb);
+        // base^(gamma-1) = s / base (base > 0)
+        rb[e + q] = cts * gamma * (s / base) * fact;
       }
     }
   }
-  block_reduce_store<1>(acc, partials, 1);
+  block_reduce_kahan<1>(acc, partials, 1);
 }
 
 // Adjoint z pass of the three cotangent channels: r2c rows of the float4 mesh.
@@ -713,7 +738,7 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
               nu = __ldg(params + 4);
   const float a1 = 1e-2f * scale;  // d P / d alpha = 1e-2 G S / Nc
   const int nz = 2 * sp.h, nyy = sp.ny;
-  double acc[4] = {0, 0, 0, 0};
+  KahanF acc[4];
   for (int f = tid; f < cols * n; f += nthr) {
     int c = f & (cols - 1), j = f >> sp.cshift;
     int64_t ad = colad[c];
@@ -732,11 +757,11 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
       float mk = (kz == 0 || (kz == sp.h && (nz & 1) == 0)) ? 1.f : 2.f;
       float m_alpha = mode == 1 ? mk : 1.f;
       float m_green = mode == 1 ? mk : ((kz >= 1 && kz < nyy / 2) ? 2.f : 1.f);
-      acc[0] += (double)(m_alpha * a1) * gr.g * reWS;
+      acc[0].add(m_alpha * a1 * gr.g * reWS);
       float qg = m_green * 1e-2f * alpha * scale * reWS;
-      acc[1] += (double)qg * gr.dkh;
-      acc[2] += (double)qg * gr.dkl;
-      acc[3] += (double)qg * gr.dnu;
+      acc[1].add(qg * gr.dkh);
+      acc[2].add(qg * gr.dkl);
+      acc[3].add(qg * gr.dnu);
       float vm = 1e-2f * alpha * scale * gr.g;
       v = make_float2(W.x * vm, W.y * vm);
     }
@@ -745,34 +770,41 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
   __syncthreads();
   fft_tile<float, SCHED>(s0, ld, pl, sp.cshift, +1, tid, nthr);
   tile_store(s0, ld, Vout, colad, es, n, cols, sp.cshift, tid, nthr);
-  block_reduce_store<4>(acc, partials, 4);
+  block_reduce_kahan<4>(acc, partials, 4);
 }
 
 // Sums per-block partials in a fixed order: out[slot] = sum_b partials[b*stride + j].
-// scale_ptr (device, may be null) multiplies the sums.
-__global__ void finish_kernel(const double* __restrict__ partials, int nblocks, int stride,
-                              int nvals, double* __restrict__ out, int out_off,
-                              const double* __restrict__ scale_ptr) {
-  int j = threadIdx.x;
-  if (j < nvals) {
-    double s = 0;
-    for (int b = 0; b < nblocks; ++b) s += partials[(int64_t)b * stride + j];
-    out[out_off + j] = scale_ptr ? s * scale_ptr[0] : s;
+// One block per value j, 256 threads, fixed summation order (strided
+// per-thread sums, then a shared-memory tree), so results are reproducible.
+// scale_ptr (device, may be null) multiplies the sum; invert != 0 stores 1/sum.
+__global__ void __launch_bounds__(256)
+finish_kernel(const double* __restrict__ partials, int nblocks, int stride, int nvals,
+              double* __restrict__ out, int out_off, const double* __restrict__ scale_ptr,
+              int invert) {
+  __shared__ double sh[256];
+  const int j = blockIdx.x;
+  double s = 0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(int64_t)b * stride + j];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && j < nvals) {
+    double v = sh[0];
+    if (scale_ptr) v *= scale_ptr[0];
+    out[out_off + j] = invert ? 1.0 / v : v;
   }
 }
 
 // Sum of the mask in FP64 (Npixel) and its reciprocal.
 __global__ void mask_count_kernel(const float* __restrict__ mask, int64_t C, double* __restrict__ partials) {
-  double acc[1] = {0};
+  KahanF acc[1];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < C;
        e += (int64_t)gridDim.x * blockDim.x)
-    acc[0] += (double)__ldg(mask + e);
-  block_reduce_store<1>(acc, partials, 1);
-}
-__global__ void inv_kernel(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
-  double s = 0;
-  for (int b = 0; b < nblocks; ++b) s += partials[b];
-  out[0] = 1.0 / s;
+    acc[0].add(__ldg(mask + e));
+  block_reduce_kahan<1>(acc, partials, 1);
 }
 __global__ void set_scalar_kernel(double* out, double v) { out[0] = v; }
 
