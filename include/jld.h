@@ -237,7 +237,8 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /*   L1      1: sum |F - target| (model default for "sm"), 0: squares      */
 /*   grad_mode 0: the reference's VJP rules, 1: exact adjoint (differs    */
 /*           from 0 only in d/d alpha)                                     */
-/*   paint_method 0: atomics, 1: warp-aggregated atomics                   */
+/*   options bit 0: warp-aggregated paint atomics (else plain atomics);   */
+/*           bit 1: generic pass kernels instead of the TMA-pipelined ones */
 /*   out     device float64: [loss, d loss / d params ...]                 */
 /* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
 /* into a CUDA graph; parameters are read from device memory, so a graph  */
@@ -248,8 +249,12 @@ JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float 
 JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts,
                              int32_t nx, int32_t ny, int32_t nz, const float box[3],
                              int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
-                             int32_t paint_method, const float* params, const float* target,
+                             int32_t options, const float* params, const float* target,
                              const float* mask, void* ws, size_t ws_bytes, double* out);
+/* Device pointer to the step's error word in `ws` (0 = fine; nonzero = a  */
+/* pipelined pass gave up waiting for a tile copy and stopped early).      */
+JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,
+                                   int64_t nparts, int32_t nstep, const int** out);
 /* Device pointer to the positions after `layer` (1..nstep) layers of the */
 /* last step run on `ws`.                                                  */
 JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,

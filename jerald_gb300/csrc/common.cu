@@ -5,6 +5,10 @@
 
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace jld {
 
 static thread_local char g_msg[512] = "";
@@ -29,6 +33,22 @@ int sm_count() {
     n = 148;
   if (dev >= 0 && dev < 64) cached[dev] = n;
   return n;
+}
+
+int ensure_smem_ptr(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  JLD_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_pair(func, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return JLD_OK;
+  const size_t lim = 227 * 1024;
+  if (bytes > lim) return set_error(JLD_ERR_UNSUPPORTED, "kernel needs %zu bytes of shared memory", bytes);
+  JLD_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim));
+  done[key] = lim;
+  return JLD_OK;
 }
 
 }  // namespace jld

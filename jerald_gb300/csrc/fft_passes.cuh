@@ -9,19 +9,15 @@
 
 namespace jld {
 
-// Sets the dynamic shared-memory limit of `func` on the current device the
-// first time a launch needs more than the 48 KB default.
+// Raises the dynamic shared-memory limit of kernel `func` on the current
+// device (once per kernel and device) when a launch needs more than the
+// 48 KB default.
+int ensure_smem_ptr(const void* func, size_t bytes);
+
 template <typename F>
 inline int ensure_smem(F func, size_t bytes) {
   if (bytes <= 48 * 1024) return JLD_OK;
-  static int done[64] = {0};
-  int dev = 0;
-  JLD_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 64 && done[dev] >= (int)bytes) return JLD_OK;
-  JLD_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    200 * 1024));
-  if (dev < 64) done[dev] = 200 * 1024;
-  return JLD_OK;
+  return ensure_smem_ptr(reinterpret_cast<const void*>(func), bytes);
 }
 
 inline int ilog2i(int v) { int s = 0; while ((1 << s) < v) ++s; return s; }

@@ -1,0 +1,261 @@
+// Pipelined pencil-FFT passes for power-of-two line lengths (sm_103a).
+//
+// Persistent CTAs walk a stream of "items" (one input tile each).  A ring of
+// shared-memory staging slots is filled by the Tensor Memory Accelerator:
+// cp.async.bulk.tensor (2-D/3-D tiles of strided pencils) or cp.async.bulk
+// (contiguous rows), each completing on an mbarrier with its byte count.
+// While a CTA transforms item i, the loads of items i+1 .. i+NSLOT-1 are in
+// flight.  The transform itself uses a compile-time radix schedule (P2<...>):
+// its first stage reads the staging slot (or any functor), its middle stages
+// go through a work buffer, its last stage hands every value to an output
+// functor (usually a direct, coalesced global store with the elementwise
+// epilogue of the pass applied in registers).
+//
+// Every mbarrier wait is bounded: after kWaitLimit polls the CTA records an
+// error in the pass's error word and stops, so a lost copy cannot hang the GPU.
+#pragma once
+
+#include <cuda.h>  // CUtensorMap (type only; the encoder is resolved at run time)
+
+#include "fft_core.cuh"
+
+namespace jld {
+
+// ---------------------------------------------------------------------------
+// PTX helpers.
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+constexpr int kWaitLimit = 1 << 22;
+
+// Bounded wait on `parity` of an mbarrier; false after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Orders earlier generic-proxy accesses of shared memory before a later TMA
+// (async-proxy) write into it.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Compile-time power-of-two schedules (radix of the first stage first).
+constexpr int cmax_pack(int a) { return a; }
+template <class... Ts>
+constexpr int cmax_pack(int a, Ts... r) {
+  int b = cmax_pack(r...);
+  return a > b ? a : b;
+}
+constexpr int clog2(int v) {
+  int s = 0;
+  while ((1 << s) < v) ++s;
+  return s;
+}
+
+template <int... Rs>
+struct P2 {
+  static constexpr int nst = sizeof...(Rs);
+  static constexpr int rad[nst] = {Rs...};
+  static constexpr int n = (1 * ... * Rs);
+  static constexpr int E = cmax_pack(Rs...);
+  static constexpr int pre(int s) {
+    int p = 1;
+    for (int i = 0; i < s; ++i) p *= rad[i];
+    return p;
+  }
+};
+
+// Work-buffer layouts.
+//   ColWork: element (c, j) at j * cols + c   (strided passes: threads c-fastest)
+//   RowWork: element (c, j) at c * ldw + j + (j >> PSH) (row passes: j-fastest;
+//            the padding keeps the first stage's stride-R writes conflict-free)
+struct ColWork {
+  float2* p;
+  int cols;
+  __device__ __forceinline__ float2& at(int c, int j) const { return p[j * cols + c]; }
+};
+template <int PSH>
+struct RowWork {
+  float2* p;
+  int ldw;
+  __device__ __forceinline__ float2& at(int c, int j) const { return p[c * ldw + j + (j >> PSH)]; }
+};
+
+// One stage S of schedule Sch over all columns of the tile.  COL selects the
+// thread mapping (c-fastest for strided tiles, j-fastest for rows).  With
+// SYNC_MID the stage loads everything, synchronises, then stores (in place).
+template <class Sch, int S, bool COL, bool SYNC_MID, class Ld, class St, class Mid>
+__device__ __forceinline__ void p2_stage(const Ld& ld, const St& st, const float2* __restrict__ tw, int sgn,
+                                         int cshift, int tid, int nthr, const Mid& mid) {
+  constexpr int R = Sch::rad[S];
+  constexpr int P = Sch::pre(S);
+  constexpr int N = Sch::n;
+  constexpr int T = N / R;
+  constexpr int Q = Sch::E / R;
+  constexpr int TWS = N / (P * R);
+  constexpr int LT = clog2(T);
+  float2 u[Q][R];
+  int cc[Q], bb[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int id = tid + q * nthr;
+    int c, b;
+    if constexpr (COL) {
+      c = id & ((1 << cshift) - 1);
+      b = id >> cshift;
+    } else {
+      b = id & (T - 1);
+      c = id >> LT;
+    }
+    cc[q] = c;
+    bb[q] = b;
+#pragma unroll
+    for (int r = 0; r < R; ++r) u[q][r] = ld(c, b + r * T);
+  }
+  if constexpr (SYNC_MID) {
+    __syncthreads();
+    mid();
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int b = bb[q], c = cc[q];
+    const int k = b & (P - 1);
+    if constexpr (P > 1) {
+      if (k != 0) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = __ldg(tw + r * k * TWS);
+          if (sgn > 0) w.y = -w.y;
+          u[q][r] = cmul(u[q][r], w);
+        }
+      }
+    }
+    dftR<R>(u[q], sgn);
+    const int j = (b - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) st(c, j + r * P, u[q][r]);
+  }
+}
+
+// Whole transform of a tile: in(c, j) -> [work] -> out(c, j, v).  `rel` runs
+// (on every thread) right after the barrier that follows the first stage,
+// i.e. once no thread reads `in` any more: the place to recycle the input's
+// staging slot.  The caller synchronises before (work / input free) and
+// after (if the output lands in shared memory that other threads read).
+struct NoRelease {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+template <class Sch, bool COL, class W, class In, class Out, class Rel>
+__device__ __forceinline__ void p2_run_rel(const W& work, const In& in, const Out& out, const Rel& rel,
+                                           const float2* __restrict__ tw, int sgn, int cshift, int tid,
+                                           int nthr) {
+  auto wld = [&](int c, int j) { return work.at(c, j); };
+  auto wst = [&](int c, int j, float2 v) { work.at(c, j) = v; };
+  if constexpr (Sch::nst == 1) {
+    p2_stage<Sch, 0, COL, true>(in, out, tw, sgn, cshift, tid, nthr, rel);
+  } else {
+    p2_stage<Sch, 0, COL, false>(in, wst, tw, sgn, cshift, tid, nthr, NoRelease{});
+    __syncthreads();
+    rel();
+    if constexpr (Sch::nst >= 3) {
+      p2_stage<Sch, 1, COL, true>(wld, wst, tw, sgn, cshift, tid, nthr, NoRelease{});
+      __syncthreads();
+    }
+    if constexpr (Sch::nst >= 4) {
+      p2_stage<Sch, 2, COL, true>(wld, wst, tw, sgn, cshift, tid, nthr, NoRelease{});
+      __syncthreads();
+    }
+    p2_stage<Sch, Sch::nst - 1, COL, false>(wld, out, tw, sgn, cshift, tid, nthr, NoRelease{});
+  }
+}
+
+template <class Sch, bool COL, class W, class In, class Out>
+__device__ __forceinline__ void p2_run(const W& work, const In& in, const Out& out, const float2* __restrict__ tw,
+                                       int sgn, int cshift, int tid, int nthr) {
+  p2_run_rel<Sch, COL>(work, in, out, NoRelease{}, tw, sgn, cshift, tid, nthr);
+}
+
+// Schedules used for each power-of-two length: radix-16 stages and one
+// smaller tail, E = 16 elements per thread per column.
+template <int N> struct P2For;
+template <> struct P2For<16> { using type = P2<16>; };
+template <> struct P2For<32> { using type = P2<16, 2>; };
+template <> struct P2For<64> { using type = P2<16, 4>; };
+template <> struct P2For<128> { using type = P2<16, 8>; };
+template <> struct P2For<256> { using type = P2<16, 16>; };
+template <> struct P2For<512> { using type = P2<16, 16, 2>; };
+template <> struct P2For<1024> { using type = P2<16, 16, 4>; };
+template <> struct P2For<2048> { using type = P2<16, 16, 8>; };
+
+// Calls body(P2For<N>::type{}) for a supported power of two; returns -1 if
+// n has no pipelined schedule.
+template <class F>
+inline int with_p2(int n, F&& body) {
+  switch (n) {
+    case 16: return body(P2For<16>::type{});
+    case 32: return body(P2For<32>::type{});
+    case 64: return body(P2For<64>::type{});
+    case 128: return body(P2For<128>::type{});
+    case 256: return body(P2For<256>::type{});
+    case 512: return body(P2For<512>::type{});
+    case 1024: return body(P2For<1024>::type{});
+    case 2048: return body(P2For<2048>::type{});
+    default: return -1;
+  }
+}
+
+}  // namespace jld

@@ -7,15 +7,97 @@
 
 #include <algorithm>
 
+#include <cudaTypedefs.h>
+
 #include "ldl_kernels.cuh"
+#include "ldl_pipe.cuh"
 
 namespace jld {
+
+// ---------------------------------------------------------------------------
+// TMA descriptors for the pipelined passes.
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+// Tensor map over the main block main[nx][ny][h] (complex, viewed as float
+// pairs) with a box of `cols` columns by min(lines, 256) lines.
+static int make_main_map(CUtensorMap* m, const float2* main, int nx, int ny, int h, int ax, int cols,
+                         int lines) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return set_error(JLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const cuuint32_t boxl = (cuuint32_t)std::min(lines, 256);
+  CUresult r;
+  if (ax == 1) {
+    cuuint64_t dims[3] = {(cuuint64_t)2 * h, (cuuint64_t)ny, (cuuint64_t)nx};
+    cuuint64_t strides[2] = {(cuuint64_t)h * 8, (cuuint64_t)ny * h * 8};
+    cuuint32_t box[3] = {(cuuint32_t)(2 * cols), boxl, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)main, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  } else {
+    cuuint64_t dims[2] = {(cuuint64_t)2 * ny * h, (cuuint64_t)nx};
+    cuuint64_t strides[1] = {(cuuint64_t)ny * h * 8};
+    cuuint32_t box[2] = {(cuuint32_t)(2 * cols), boxl};
+    cuuint32_t es[2] = {1, 1};
+    r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)main, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  }
+  if (r != CUDA_SUCCESS) return set_error(JLD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return JLD_OK;
+}
+
+// Geometry of a pipelined strided pass over the main block, or ok = false
+// when the mesh does not qualify (line length not a power of two in
+// [16, 2048], or h not a multiple of the tile width).
+struct PipeGeom {
+  bool ok = false;
+  SGeom g;
+  int nthr = 0;
+  int grid = 0;
+  size_t smem = 0;
+};
+
+static PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc) {
+  PipeGeom p;
+  const int lines = ax == 1 ? ny : nx;
+  if (lines < 16 || lines > 2048 || (lines & (lines - 1)) || h < 2 || (h & 1)) return p;
+  int cols = 16;
+  while (cols > 1 && (cols * lines / 16 > 512 || (size_t)lines * cols * 8 > 64 * 1024)) cols >>= 1;
+  while (cols > 1 && h % cols) cols >>= 1;
+  if (cols < 4) return p;
+  SGeom& g = p.g;
+  g.nx = nx; g.ny = ny; g.h = h;
+  g.cols = cols;
+  g.cshift = ilog2i(cols);
+  g.lines = lines;
+  g.ntiles = (int)(((int64_t)(ax == 1 ? nx : ny) * h) / cols);
+  g.es = ax == 1 ? h : (int64_t)ny * h;
+  p.nthr = cols * lines / 16;
+  p.grid = std::min(g.ntiles, sm_count());
+  p.smem = (size_t)lines * cols * 8 * (2 + nacc) + 64;
+  p.ok = true;
+  return p;
+}
 
 struct LdlLayout {
   int64_t N, C, H;
   int nstep;
   size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
-      off_npix, total;
+      off_npix, off_err, total;
   int64_t part_doubles;
 };
 
@@ -42,6 +124,7 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
   L.off_rb = o; o += al(sizeof(float) * L.C);                  // density cotangent
   L.off_part = o; o += al(sizeof(double) * L.part_doubles);    // per-block FP64 partials
   L.off_npix = o; o += al(sizeof(double) * 2);                 // 1 / Npixel
+  L.off_err = o; o += al(sizeof(int) * 4);                     // pipelined-pass error word
   L.total = o;
   return L;
 }
@@ -51,6 +134,7 @@ struct StepArgs {
   const float* pos0; int64_t N;
   int nx, ny, nz; float box[3];
   int nstep, kind, L1, mode, paint_method;
+  bool use_pipe;         // TMA-pipelined strided passes where the mesh qualifies
   const float* params;   // device: 5*nstep (+3 for kind 0)
   const float* target; const float* mask;
   char* ws;
@@ -150,6 +234,50 @@ static int ldl_step(const StepArgs& a) {
     JLD_LAUNCH_CHECK("set_scalar_kernel");
   }
 
+  // ---------------- pipelined (TMA-staged) strided passes, when the mesh qualifies
+  int* err = (int*)(ws + L.off_err);
+  JLD_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int) * 4, st));
+  const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0), py1 = pipe_geom(nx, ny, h, 1, 1);
+  const PipeGeom px1 = pipe_geom(nx, ny, h, 0, 1);
+  const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
+  // the generic kernels then only cover the nyq plane
+  SpecPass gxn = gx.sp, gyn = gy.sp;
+  gxn.tiles_main = 0;
+  gyn.tiles_main = 0;
+  const unsigned gxn_tiles = (unsigned)((ny + gx.sp.cols - 1) / gx.sp.cols);
+  const unsigned gyn_tiles = (unsigned)((nx + gy.sp.cols - 1) / gy.sp.cols);
+  auto ymap = [&](CUtensorMap* m, const float2* B, const PipeGeom& p) {
+    return make_main_map(m, B, nx, ny, h, 1, p.g.cols, ny);
+  };
+  auto xmap = [&](CUtensorMap* m, const float2* B, const PipeGeom& p) {
+    return make_main_map(m, B, nx, ny, h, 0, p.g.cols, nx);
+  };
+  // y FFT in place on buffer B (main + nyq).
+  auto ypass = [&](float2* B, int sgn) -> int {
+    if (!pipe) return launch_y_pass<float>(st, pl, B, B + nyq_off, sgn);
+    CUtensorMap m;
+    int e = ymap(&m, B, py0);
+    if (e) return e;
+    e = with_p2(ny, [&](auto sch) {
+      using Sch = decltype(sch);
+      auto kern = sgn < 0 ? spass_kernel<Sch, 1, -1> : spass_kernel<Sch, 1, 1>;
+      int r = ensure_smem(kern, py0.smem);
+      if (r) return r;
+      kern<<<py0.grid, py0.nthr, py0.smem, st>>>(m, B, py0.g, pl.py.tw, err);
+      return 0;
+    });
+    if (e) return e;
+    JLD_LAUNCH_CHECK("spass_kernel");
+    LineJob<float> jn, none;
+    float2* nq = B + nyq_off;
+    jn.src = nq; jn.dst = nq;
+    jn.es_in = jn.es_out = 1;
+    jn.cdiv_in = jn.cdiv_out = 1;
+    jn.cmul_in = jn.cmul_out = ny;
+    jn.ncol = nx;
+    return launch_line_pass<float>(st, pl.py, jn, none, sgn);
+  };
+
   // ---------------- forward layers
   for (int l = 0; l < a.nstep; ++l) {
     const float* prm = a.params + 5 * l;
@@ -159,23 +287,51 @@ static int ldl_step(const StepArgs& a) {
     if ((s = paint_unit_f32(st, Xl(l), a.N, nx, ny, nz, a.box, a.paint_method, rho_l))) return s;
     SourcePow src{prm, fact};
     if ((s = launch_rfft_z_src<float, SourcePow>(st, pl, rho_l, src, W[0], W[0] + nyq_off))) return s;
-    if ((s = launch_y_pass<float>(st, pl, W[0], W[0] + nyq_off, -1))) return s;
+    if ((s = ypass(W[0], -1))) return s;
+    if (pipe) {
+      CUtensorMap mA;
+      if ((s = xmap(&mA, W[0], px1))) return s;
+      s = with_p2(nx, [&](auto sch) {
+        using Sch = decltype(sch);
+        int r = ensure_smem(xfilt_pipe_kernel<Sch>, px1.smem);
+        if (r) return r;
+        xfilt_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(mA, px1.g, kt, prm, a.kind, scale, S_l, W[1],
+                                                                    W[2], pl.px.tw, err);
+        return 0;
+      });
+      if (s) return s;
+      JLD_LAUNCH_CHECK("xfilt_pipe_kernel");
+    }
     s = with_sched(pl.px, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(xfilt_kernel<SC>, 2 * gx.smem1);
       if (e) return e;
-      xfilt_kernel<SC><<<(unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(pl.px, gx.sp, kt, prm, a.kind, scale,
-                                                                          W[0], S_l, W[1], W[2]);
+      xfilt_kernel<SC><<<pipe ? gxn_tiles : (unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(
+          pl.px, pipe ? gxn : gx.sp, kt, prm, a.kind, scale, W[0], S_l, W[1], W[2]);
       return 0;
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("xfilt_kernel");
+    if (pipe) {
+      CUtensorMap m0, m1;
+      if ((s = ymap(&m0, W[1], py0)) || (s = ymap(&m1, W[2], py0))) return s;
+      s = with_p2(ny, [&](auto sch) {
+        using Sch = decltype(sch);
+        int r = ensure_smem(yinv3_pipe_kernel<Sch>, py0.smem);
+        if (r) return r;
+        yinv3_pipe_kernel<Sch><<<py0.grid, py0.nthr, py0.smem, st>>>(m0, m1, py0.g, kt, W[3], W[0], W[4],
+                                                                    pl.py.tw, err);
+        return 0;
+      });
+      if (s) return s;
+      JLD_LAUNCH_CHECK("yinv3_pipe_kernel");
+    }
     s = with_sched(pl.py, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(yinv3_kernel<SC>, gy.smem1);
       if (e) return e;
-      yinv3_kernel<SC><<<(unsigned)gy.tiles, gy.nthr, gy.smem1, st>>>(pl.py, gy.sp, kt, W[1], W[2], W[3], W[0],
-                                                                      W[4]);
+      yinv3_kernel<SC><<<pipe ? gyn_tiles : (unsigned)gy.tiles, gy.nthr, gy.smem1, st>>>(
+          pl.py, pipe ? gyn : gy.sp, kt, W[1], W[2], W[3], W[0], W[4]);
       return 0;
     });
     if (s) return s;
@@ -224,30 +380,64 @@ static int ldl_step(const StepArgs& a) {
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("zfwd3_kernel");
+    if (pipe) {
+      CUtensorMap m0, m1, m2;
+      if ((s = ymap(&m0, W[0], py1)) || (s = ymap(&m1, W[1], py1)) || (s = ymap(&m2, W[2], py1))) return s;
+      s = with_p2(ny, [&](auto sch) {
+        using Sch = decltype(sch);
+        int r = ensure_smem(yfwd_comb_pipe_kernel<Sch>, py1.smem);
+        if (r) return r;
+        yfwd_comb_pipe_kernel<Sch><<<py1.grid, py1.nthr, py1.smem, st>>>(m0, m1, m2, py1.g, kt, W[0], W[3],
+                                                                        pl.py.tw, err);
+        return 0;
+      });
+      if (s) return s;
+      JLD_LAUNCH_CHECK("yfwd_comb_pipe_kernel");
+    }
     s = with_sched(pl.py, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(yfwd_comb_kernel<SC>, 2 * gy.smem1);
       if (e) return e;
-      yfwd_comb_kernel<SC><<<(unsigned)gy.tiles, gy.nthr, 2 * gy.smem1, st>>>(pl.py, gy.sp, kt, W[0], W[1],
-                                                                               W[2], W[3]);
+      yfwd_comb_kernel<SC><<<pipe ? gyn_tiles : (unsigned)gy.tiles, gy.nthr, 2 * gy.smem1, st>>>(
+          pl.py, pipe ? gyn : gy.sp, kt, W[0], W[1], W[2], W[3]);
       return 0;
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("yfwd_comb_kernel");
+    // x adjoint: partial sums of the pipelined kernel first, the nyq plane's after them
+    int nparts_x = 0;
+    if (pipe) {
+      CUtensorMap m0, m1, m2;
+      if ((s = xmap(&m0, W[0], px1)) || (s = xmap(&m1, W[3], px1)) || (s = xmap(&m2, S_l, px1))) return s;
+      s = with_p2(nx, [&](auto sch) {
+        using Sch = decltype(sch);
+        int r = ensure_smem(xbwd_pipe_kernel<Sch>, px1.smem);
+        if (r) return r;
+        xbwd_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(m0, m1, m2, px1.g, kt, prm, a.kind, a.mode,
+                                                                   scale, W[1], part, pl.px.tw, err);
+        return 0;
+      });
+      if (s) return s;
+      JLD_LAUNCH_CHECK("xbwd_pipe_kernel");
+      nparts_x = px1.grid;
+    }
+    const unsigned xb_grid = pipe ? gxn_tiles : (unsigned)gx.tiles;
     s = with_sched(pl.px, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(xbwd_kernel<SC>, 2 * gx.smem1);
       if (e) return e;
-      xbwd_kernel<SC><<<(unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(pl.px, gx.sp, kt, prm, a.kind, a.mode,
-                                                                         scale, W[0], W[3], S_l, W[1], part);
+      xbwd_kernel<SC><<<xb_grid, gx.nthr, 2 * gx.smem1, st>>>(pl.px, pipe ? gxn : gx.sp, kt, prm, a.kind, a.mode,
+                                                               scale, W[0], W[3], S_l, W[1],
+                                                               part + (size_t)4 * nparts_x);
       return 0;
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("xbwd_kernel");
+    nparts_x += (int)xb_grid;
     // d alpha -> out[1+5l], d kh, d kl, d nu -> out[1+5l+2 .. 4]
-    launch_finish(st, part, (int)gx.tiles, 4, 1, a.out, 1 + 5 * l, nullptr);
-    launch_finish(st, part + 1, (int)gx.tiles, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
-    if ((s = launch_y_pass<float>(st, pl, W[1], W[1] + nyq_off, +1))) return s;
+    launch_finish(st, part, nparts_x, 4, 1, a.out, 1 + 5 * l, nullptr);
+    launch_finish(st, part + 1, nparts_x, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
+    if ((s = ypass(W[1], +1))) return s;
     s = with_sched(pl.pz, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(zinv_adj_kernel<SC>, smz);
@@ -302,7 +492,7 @@ JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float 
 
 JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
                              int32_t nz, const float box[3], int32_t nstep, int32_t kind, int32_t L1,
-                             int32_t grad_mode, int32_t paint_method, const float* params,
+                             int32_t grad_mode, int32_t options, const float* params,
                              const float* target, const float* mask, void* ws, size_t ws_bytes,
                              double* out) {
   clear_error();
@@ -313,8 +503,8 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
   if (grad_mode != 0 && grad_mode != 1)
     return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
-  if (paint_method != 0 && paint_method != 1)
-    return set_error(JLD_ERR_ARG, "%s: paint_method must be 0 or 1", who);
+  if (options & ~3) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
+  const int paint_method = options & 1;
   if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
   size_t need = ldl_layout(nx, ny, nz, nparts, nstep).total;
   if (!ws || ws_bytes < need)
@@ -326,9 +516,19 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   a.nx = nx; a.ny = ny; a.nz = nz;
   for (int i = 0; i < 3; ++i) a.box[i] = box[i];
   a.nstep = nstep; a.kind = kind; a.L1 = L1; a.mode = grad_mode; a.paint_method = paint_method;
+  a.use_pipe = (options & 2) == 0;
   a.params = params; a.target = target; a.mask = mask;
   a.ws = (char*)ws; a.out = out;
   return ldl_step(a);
+}
+
+JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                                   int32_t nstep, const int** out) {
+  clear_error();
+  if (!ws || !out || nstep < 1 || nparts < 1) return set_error(JLD_ERR_ARG, "jld_ldl_error_word_f32: bad arguments");
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  *out = (const int*)((const char*)ws + L.off_err);
+  return JLD_OK;
 }
 
 JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,

@@ -29,7 +29,8 @@ _PAINT = {"atomic": 0, "warp": 1}
 
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
-                 grad_mode: str = "reference", paint_method: str = "atomic", device="cuda"):
+                 grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
+                 pipelined: bool = True):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
         self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
@@ -39,6 +40,7 @@ class FusedLDL:
         self.L1 = (kind != "dm") if L1 is None else bool(L1)
         self.grad_mode = grad_mode
         self.paint_method = paint_method
+        self.pipelined = bool(pipelined)
         self.nparts = int(nparts)
         self.nstep = int(nstep)
         self.nparams = 5 * self.nstep + (3 if kind == "sm" else 0)
@@ -69,7 +71,8 @@ class FusedLDL:
         st = ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         _lib.call("jld_ldl_step_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
                   self.box.ctypes.data_as(ct.c_void_p), self.nstep, _KINDS[self.kind], int(self.L1),
-                  _MODES[self.grad_mode], _PAINT[self.paint_method], ct.c_void_p(self.params.data_ptr()),
+                  _MODES[self.grad_mode], _PAINT[self.paint_method] | (0 if self.pipelined else 2),
+                  ct.c_void_p(self.params.data_ptr()),
                   ct.c_void_p(target.data_ptr()), ct.c_void_p(mask.data_ptr()) if mask is not None else None,
                   ct.c_void_p(self.ws.data_ptr()), self.ws.numel(), ct.c_void_p(self.out.data_ptr()))
 
@@ -105,6 +108,14 @@ class FusedLDL:
             self._set_params(params)
         self.graph.replay()
         return self.out[0], self.out[1:]
+
+    def error_word(self) -> int:
+        """Nonzero if a pipelined pass of the last step gave up waiting for a copy."""
+        ptr = ct.c_void_p()
+        _lib.call("jld_ldl_error_word_f32", ct.c_void_p(self.ws.data_ptr()), *self.nmesh, self.nparts, self.nstep,
+                  ct.byref(ptr))
+        off = ptr.value - self.ws.data_ptr()
+        return int(self.ws[off: off + 4].view(torch.int32).item())
 
     def positions(self, layer: int) -> torch.Tensor:
         """(nparts, 3) view of the positions after `layer` layers of the last step."""

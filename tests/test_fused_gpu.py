@@ -113,6 +113,25 @@ def test_fused_graph_replay_matches_eager(paint):
     assert abs(float(l2) - float(l0)) > 1e-6 * abs(float(l0))
 
 
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_pipelined_passes_match_generic_passes(n):
+    box = 100.0
+    X, p, tgt, o, _ = _case(n, box, "sm", True, 17)
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    t = torch.from_numpy(tgt).cuda()
+    fa = _fused(n, box, len(X), "sm", True, "true")
+    from jerald_gb300.ldl import FusedLDL
+    fb = FusedLDL(n, box, len(X), nstep=2, kind="sm", grad_mode="true", pipelined=False)
+    la, ga = [v.clone() for v in fa(pos, p, t)]
+    lb, gb = [v.clone() for v in fb(pos, p, t)]
+    torch.cuda.synchronize()
+    assert fa.error_word() == 0 and fb.error_word() == 0
+    assert abs(float(la) - float(lb)) <= 1e-6 * abs(float(lb))
+    assert _rel(ga.cpu().numpy(), gb.cpu().numpy()).max() < 1e-3
+    xa, xb = fa.positions(2), fb.positions(2)
+    assert float((xa - xb).abs().max()) < 1e-4
+
+
 def test_fused_rejects_bad_arguments():
     from jerald_gb300 import _lib
     from jerald_gb300.ldl import FusedLDL
