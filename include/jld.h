@@ -239,6 +239,8 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /*           from 0 only in d/d alpha)                                     */
 /*   options bit 0: warp-aggregated paint atomics (else plain atomics);   */
 /*           bit 1: generic pass kernels instead of the TMA-pipelined ones */
+/*           bit 2: bin the particles into 16^3-cell tiles first (counting */
+/*                  sort) and scatter through shared-memory tile windows   */
 /*   out     device float64: [loss, d loss / d params ...]                 */
 /* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
 /* into a CUDA graph; parameters are read from device memory, so a graph  */
@@ -255,8 +257,12 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
 /* pipelined pass gave up waiting for a tile copy and stopped early).      */
 JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,
                                    int64_t nparts, int32_t nstep, const int** out);
+/* Device pointer to the particle order of the last step run on `ws` with */
+/* binning: entry s is the input index of the particle stored at s.        */
+JLD_API int jld_ldl_order_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                              int32_t nstep, const int** out);
 /* Device pointer to the positions after `layer` (1..nstep) layers of the */
-/* last step run on `ws`.                                                  */
+/* last step run on `ws` (in the order of jld_ldl_order_f32 when binned).  */
 JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,
                                   int64_t nparts, int32_t nstep, int32_t layer,
                                   const float** out);

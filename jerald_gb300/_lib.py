@@ -61,6 +61,7 @@ _SIGS = {
                          _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
     "jld_ldl_positions_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _i32, _c_void_p],
     "jld_ldl_error_word_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
+    "jld_ldl_order_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
 }
 _RESTYPES = {
     "jld_version": ct.c_char_p,

@@ -44,10 +44,15 @@ int ensure_smem_ptr(const void* func, size_t bytes) {
   auto key = std::make_pair(func, dev);
   auto it = done.find(key);
   if (it != done.end() && it->second >= bytes) return JLD_OK;
-  const size_t lim = 227 * 1024;
-  if (bytes > lim) return set_error(JLD_ERR_UNSUPPORTED, "kernel needs %zu bytes of shared memory", bytes);
-  JLD_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim));
-  done[key] = lim;
+  // The limit is per kernel (the opt-in maximum minus the kernel's static
+  // shared memory), so raise it exactly to what this launch needs.
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return set_error(JLD_ERR_UNSUPPORTED, "kernel cannot get %zu bytes of dynamic shared memory: %s", bytes,
+                     cudaGetErrorString(e));
+  }
+  done[key] = bytes;
   return JLD_OK;
 }
 

@@ -9,6 +9,7 @@
 
 #include <cudaTypedefs.h>
 
+#include "bins.cuh"
 #include "ldl_kernels.cuh"
 #include "ldl_pipe.cuh"
 
@@ -97,12 +98,14 @@ struct LdlLayout {
   int64_t N, C, H;
   int nstep;
   size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
-      off_npix, off_err, total;
+      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, total;
+  TileGeom tg;
   int64_t part_doubles;
 };
 
 static size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
 static constexpr int kMaxCellBlocks = 8192;
+static constexpr int kTileCells = 16;  // binning tile edge (cells)
 
 static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
   LdlLayout L;
@@ -125,6 +128,12 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
   L.off_part = o; o += al(sizeof(double) * L.part_doubles);    // per-block FP64 partials
   L.off_npix = o; o += al(sizeof(double) * 2);                 // 1 / Npixel
   L.off_err = o; o += al(sizeof(int) * 4);                     // pipelined-pass error word
+  // particle binning: tile-ordered X_0, tile keys, order, tile counts/starts/fill
+  L.tg = make_tile_geom(nx, ny, nz, kTileCells, 1);
+  L.off_xs0 = o; o += al(sizeof(float) * 3 * N);
+  L.off_keys = o; o += al(sizeof(int) * N);
+  L.off_perm = o; o += al(sizeof(int) * N);
+  L.off_tiles = o; o += al(sizeof(int) * (3 * (size_t)L.tg.ntiles() + 1));
   L.total = o;
   return L;
 }
@@ -135,6 +144,7 @@ struct StepArgs {
   int nx, ny, nz; float box[3];
   int nstep, kind, L1, mode, paint_method;
   bool use_pipe;         // TMA-pipelined strided passes where the mesh qualifies
+  bool binned;           // particles binned into tiles; tile-privatized scatters
   const float* params;   // device: 5*nstep (+3 for kind 0)
   const float* target; const float* mask;
   char* ws;
@@ -206,9 +216,42 @@ static int ldl_step(const StepArgs& a) {
   double* part = (double*)(ws + L.off_part);
   double* npix = (double*)(ws + L.off_npix);
   const int64_t nyq_off = (int64_t)nx * ny * h;
-  auto Xl = [&](int l) -> const float* { return l == 0 ? a.pos0 : Xs + (size_t)3 * a.N * (l - 1); };
   const int pblock = 256;
   const unsigned pgrid = grid_for(a.N, pblock);
+  float* Xs0 = (float*)(ws + L.off_xs0);
+  const float* X0 = a.binned ? Xs0 : a.pos0;
+  auto Xl = [&](int l) -> const float* { return l == 0 ? X0 : Xs + (size_t)3 * a.N * (l - 1); };
+  const TileGeom& tg = L.tg;
+  int* tcounts = (int*)(ws + L.off_tiles);
+  int* tstarts = tcounts + tg.ntiles();
+  int* tfill = tstarts + tg.ntiles() + 1;
+  const float3 boxv = make_float3(bg.box[0], bg.box[1], bg.box[2]);
+  const float3 cellv = make_float3(bg.cell[0], bg.cell[1], bg.cell[2]);
+  const float3 dwv = make_float3(bg.dw[0], bg.dw[1], bg.dw[2]);
+  const size_t win1 = sizeof(float) * tg.wcells(), win3 = 3 * win1;
+  const unsigned tgrid = (unsigned)std::min<int64_t>(tg.ntiles(), (int64_t)sm_count() * 8);
+  // Unit-mass paint of layer positions X into out (zeroed here).
+  auto paint_into = [&](const float* X, float* out) -> int {
+    if (!a.binned) return paint_unit_f32(st, X, a.N, nx, ny, nz, a.box, a.paint_method, out);
+    JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * L.C, st));
+    int e = ensure_smem(tiled_paint_kernel, win1);
+    if (e) return e;
+    tiled_paint_kernel<<<tgrid, 256, win1, st>>>(X, tstarts, tg, boxv, cellv, g, out);
+    JLD_LAUNCH_CHECK("tiled_paint_kernel");
+    return JLD_OK;
+  };
+  // Bin X_0 into tiles (counting sort); every layer then runs in tile order.
+  if (a.binned) {
+    JLD_CUDA_TRY(cudaMemsetAsync(tcounts, 0, sizeof(int) * tg.ntiles(), st));
+    int* keys = (int*)(ws + L.off_keys);
+    int* perm = (int*)(ws + L.off_perm);
+    bin_count_kernel<<<pgrid, pblock, 0, st>>>(a.pos0, a.N, boxv, cellv, g, tg, keys, tcounts);
+    JLD_LAUNCH_CHECK("bin_count_kernel");
+    bin_scan_kernel<<<1, 1024, 0, st>>>(tcounts, tg.ntiles(), tstarts, tfill);
+    JLD_LAUNCH_CHECK("bin_scan_kernel");
+    bin_scatter_kernel<<<pgrid, pblock, 0, st>>>(a.pos0, a.N, keys, tfill, Xs0, perm);
+    JLD_LAUNCH_CHECK("bin_scatter_kernel");
+  }
   const int cblock = 256;
   const unsigned cgrid = (unsigned)std::min<int64_t>(kMaxCellBlocks, grid_for(L.C, cblock));
   const int64_t rows = (int64_t)nx * ny;
@@ -284,7 +327,7 @@ static int ldl_step(const StepArgs& a) {
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
     float4* g4_l = g4 + (size_t)L.C * l;
-    if ((s = paint_unit_f32(st, Xl(l), a.N, nx, ny, nz, a.box, a.paint_method, rho_l))) return s;
+    if ((s = paint_into(Xl(l), rho_l))) return s;
     SourcePow src{prm, fact};
     if ((s = launch_rfft_z_src<float, SourcePow>(st, pl, rho_l, src, W[0], W[0] + nyq_off))) return s;
     if ((s = ypass(W[0], -1))) return s;
@@ -352,7 +395,7 @@ static int ldl_step(const StepArgs& a) {
 
   // ---------------- final map, loss and its cotangent
   float* rho_f = rho + (size_t)L.C * a.nstep;
-  if ((s = paint_unit_f32(st, Xl(a.nstep), a.N, nx, ny, nz, a.box, a.paint_method, rho_f))) return s;
+  if ((s = paint_into(Xl(a.nstep), rho_f))) return s;
   loss_kernel<<<cgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
                                         a.L1, npix, rb, part);
   JLD_LAUNCH_CHECK("loss_kernel");
@@ -368,8 +411,14 @@ static int ldl_step(const StepArgs& a) {
     float2* S_l = Sbuf + (size_t)L.H * l;
     float4* g4_l = g4 + (size_t)L.C * l;
     JLD_CUDA_TRY(cudaMemsetAsync(gb4, 0, sizeof(float4) * L.C, st));
-    bwd_particles_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
-    JLD_LAUNCH_CHECK("bwd_particles_kernel");
+    if (a.binned) {
+      if ((s = ensure_smem(tiled_bwd_kernel, win3))) return s;
+      tiled_bwd_kernel<<<tgrid, 256, win3, st>>>(Xl(l), Xb, tstarts, tg, boxv, cellv, dwv, g, g4_l, gb4, Xb2);
+      JLD_LAUNCH_CHECK("tiled_bwd_kernel");
+    } else {
+      bwd_particles_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
+      JLD_LAUNCH_CHECK("bwd_particles_kernel");
+    }
     s = with_sched(pl.pz, [&](auto sc) {
       constexpr int SC = decltype(sc)::value;
       int e = ensure_smem(zfwd3_kernel<SC>, 3 * smz);
@@ -503,7 +552,9 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
   if (grad_mode != 0 && grad_mode != 1)
     return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
-  if (options & ~3) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
+  if (options & ~7) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
+  if ((options & 4) && nparts > INT32_MAX)
+    return set_error(JLD_ERR_UNSUPPORTED, "%s: binning needs fewer than 2^31 particles", who);
   const int paint_method = options & 1;
   if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
   size_t need = ldl_layout(nx, ny, nz, nparts, nstep).total;
@@ -517,6 +568,7 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   for (int i = 0; i < 3; ++i) a.box[i] = box[i];
   a.nstep = nstep; a.kind = kind; a.L1 = L1; a.mode = grad_mode; a.paint_method = paint_method;
   a.use_pipe = (options & 2) == 0;
+  a.binned = (options & 4) != 0;
   a.params = params; a.target = target; a.mask = mask;
   a.ws = (char*)ws; a.out = out;
   return ldl_step(a);
@@ -528,6 +580,15 @@ JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32
   if (!ws || !out || nstep < 1 || nparts < 1) return set_error(JLD_ERR_ARG, "jld_ldl_error_word_f32: bad arguments");
   LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
   *out = (const int*)((const char*)ws + L.off_err);
+  return JLD_OK;
+}
+
+JLD_API int jld_ldl_order_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                              int32_t nstep, const int** out) {
+  clear_error();
+  if (!ws || !out || nstep < 1 || nparts < 1) return set_error(JLD_ERR_ARG, "jld_ldl_order_f32: bad arguments");
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  *out = (const int*)((const char*)ws + L.off_perm);
   return JLD_OK;
 }
 

@@ -24,12 +24,12 @@ from . import _lib
 
 _KINDS = {"sm": 0, "dm": 1}
 _MODES = {"reference": 0, "true": 1}
-_PAINT = {"atomic": 0, "warp": 1}
+_PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 
 
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
-                 grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
+                 grad_mode: str = "reference", paint_method: str = "tiled", device="cuda",
                  pipelined: bool = True):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
@@ -123,4 +123,13 @@ class FusedLDL:
         _lib.call("jld_ldl_positions_f32", ct.c_void_p(self.ws.data_ptr()), *self.nmesh, self.nparts,
                   self.nstep, int(layer), ct.byref(ptr))
         off = ptr.value - self.ws.data_ptr()
-        return self.ws[off: off + 12 * self.nparts].view(torch.float32).view(self.nparts, 3)
+        x = self.ws[off: off + 12 * self.nparts].view(torch.float32).view(self.nparts, 3)
+        if self.paint_method != "tiled":
+            return x
+        _lib.call("jld_ldl_order_f32", ct.c_void_p(self.ws.data_ptr()), *self.nmesh, self.nparts, self.nstep,
+                  ct.byref(ptr))
+        off = ptr.value - self.ws.data_ptr()
+        perm = self.ws[off: off + 4 * self.nparts].view(torch.int32).long()
+        out = torch.empty_like(x)
+        out[perm] = x
+        return out

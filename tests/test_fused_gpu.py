@@ -91,7 +91,30 @@ def test_fused_matches_plain_primitives():
     assert _rel(gf.cpu().numpy(), gp.cpu().numpy()).max() < 5e-3
 
 
-@pytest.mark.parametrize("paint", ["atomic", "warp"])
+def test_tiled_scatters_match_atomic_scatters_clustered():
+    # clustered particles (halos of many particles per cell), positions in
+    # input order and well outside the box
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    n, box = 64, 100.0
+    X = synth.clustered(n, box, seed=4, extra_frac=0.3, nhalo=20).astype(np.float32)
+    X[:100] += 3 * box
+    X[100:200] -= 2.5 * box
+    pos = torch.from_numpy(X).cuda()
+    t = torch.ones((n, n, n), device="cuda")
+    p = synth.default_params(2)
+    out = {}
+    for m in ("atomic", "tiled"):
+        f = FusedLDL(n, box, len(X), nstep=2, kind="sm", grad_mode="true", paint_method=m)
+        lo, g = f(pos, p, t)
+        torch.cuda.synchronize()
+        out[m] = (float(lo), g.cpu().numpy(), f.positions(2).clone())
+    assert abs(out["tiled"][0] - out["atomic"][0]) <= 1e-5 * abs(out["atomic"][0])
+    assert _rel(out["tiled"][1], out["atomic"][1]).max() < 1e-3
+    assert float((out["tiled"][2] - out["atomic"][2]).abs().max()) < 1e-3
+
+
+@pytest.mark.parametrize("paint", ["atomic", "warp", "tiled"])
 def test_fused_graph_replay_matches_eager(paint):
     n, box = 32, 100.0
     X, p, tgt, o, _ = _case(n, box, "sm", True, 13)
