@@ -306,7 +306,7 @@ def main():
                     help="run only eager fused steps (warmup + steps) on the workload, for ncu")
     ap.add_argument("--precision", action="store_true",
                     help="compare the fused FP32 step with the FP64 primitive pipeline on the workload")
-    ap.add_argument("--paint", default="atomic", choices=["atomic", "warp"])
+    ap.add_argument("--paint", default="atomic", choices=["atomic", "warp", "tiled"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -337,7 +337,8 @@ def main():
     pos, box = make_workload(n, dev, seed=rank)
     target = make_target(pos, n, box, params, dev)
     N = pos.shape[0]
-    step = FusedLDL(n, box, N, nstep=2, kind="sm", L1=True, grad_mode="reference", device=dev)
+    step = FusedLDL(n, box, N, nstep=2, kind="sm", L1=True, grad_mode="reference", paint_method=args.paint,
+                    device=dev)
     step(pos, params, target)
     step.capture(pos, target)
     for _ in range(args.warmup):

@@ -29,7 +29,7 @@ _PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
-                 grad_mode: str = "reference", paint_method: str = "tiled", device="cuda",
+                 grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
                  pipelined: bool = True):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)

@@ -138,13 +138,15 @@ def test_fused_graph_replay_matches_eager(paint):
 
 @pytest.mark.parametrize("n", [32, 64, 128])
 def test_pipelined_passes_match_generic_passes(n):
+    # L2 loss: with L1, rounding-level differences between two valid FP32
+    # forward paths flip sign(F - t) in a few cells and move d/db visibly
     box = 100.0
-    X, p, tgt, o, _ = _case(n, box, "sm", True, 17)
+    X, p, tgt, o, _ = _case(n, box, "sm", False, 17)
     pos = torch.from_numpy(X.astype(np.float32)).cuda()
     t = torch.from_numpy(tgt).cuda()
-    fa = _fused(n, box, len(X), "sm", True, "true")
+    fa = _fused(n, box, len(X), "sm", False, "true")
     from jerald_gb300.ldl import FusedLDL
-    fb = FusedLDL(n, box, len(X), nstep=2, kind="sm", grad_mode="true", pipelined=False)
+    fb = FusedLDL(n, box, len(X), nstep=2, kind="sm", L1=False, grad_mode="true", pipelined=False)
     la, ga = [v.clone() for v in fa(pos, p, t)]
     lb, gb = [v.clone() for v in fb(pos, p, t)]
     torch.cuda.synchronize()
