@@ -251,7 +251,9 @@ tiled_paint_kernel(const float* __restrict__ Xs, const int* __restrict__ starts,
 // Adjoint of one layer's readout on tile-ordered particles: Xb = Xb1 +
 // J^T Xb1 (gather of the float4 force mesh with CIC weight gradients) and the
 // three-channel scatter of Xb1 into the float4 cotangent mesh through a
-// shared-memory window (three floats per window cell).
+// shared-memory window (three floats per window cell).  GATHER = false
+// does the scatter only (the first layer).
+template <bool GATHER>
 __global__ void __launch_bounds__(256)
 tiled_bwd_kernel(const float* __restrict__ Xs, const float* __restrict__ Xb1, const int* __restrict__ starts,
                  TileGeom tg, float3 box, float3 cell, float3 dw, Grid3 g, const float4* __restrict__ g4,
@@ -293,11 +295,13 @@ tiled_bwd_kernel(const float* __restrict__ Xs, const float* __restrict__ Xb1, co
         const int gx = bx ? ci.hi[0] : ci.lo[0], gy = by ? ci.hi[1] : ci.lo[1], gz = bz ? ci.hi[2] : ci.lo[2];
         const int64_t off = (int64_t)gx * g.sx + (int64_t)gy * g.sy + gz;
         const float wx = bx ? hi[0] : lo[0], wy = by ? hi[1] : lo[1], wz = bz ? hi[2] : lo[2];
-        const float4 gv = __ldg(g4 + off);
-        const float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
-        acc[0] += u * ((bx ? dwv[0] : -dwv[0]) * wy * wz);
-        acc[1] += u * (wx * (by ? dwv[1] : -dwv[1]) * wz);
-        acc[2] += u * (wx * wy * (bz ? dwv[2] : -dwv[2]));
+        if (GATHER) {
+          const float4 gv = __ldg(g4 + off);
+          const float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
+          acc[0] += u * ((bx ? dwv[0] : -dwv[0]) * wy * wz);
+          acc[1] += u * (wx * (by ? dwv[1] : -dwv[1]) * wz);
+          acc[2] += u * (wx * wy * (bz ? dwv[2] : -dwv[2]));
+        }
         const float w = __fmul_rn(__fmul_rn(wx, wy), wz);
         const int x = bx ? wh[0] : wl[0], y = by ? wh[1] : wl[1], z = bz ? wh[2] : wl[2];
         if (x < tg.wx && y < tg.wy && z < tg.wz) {
@@ -309,8 +313,10 @@ tiled_bwd_kernel(const float* __restrict__ Xs, const float* __restrict__ Xb1, co
           atomicAdd(gb4 + off, make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f));
         }
       }
+      if (GATHER) {
 #pragma unroll
-      for (int e = 0; e < 3; ++e) Xb[p3 + e] = v[e] + acc[e];
+        for (int e = 0; e < 3; ++e) Xb[p3 + e] = v[e] + acc[e];
+      }
     }
     __syncthreads();
     for (int c = tid; c < wc; c += nthr) {

@@ -50,26 +50,47 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 
 // ---------------------------------------------------------------------------
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
+// Grid-stride loop a warp at a time (all lanes stay in the loop for the
+// pairing shuffles); lanes whose stencils share a z face merge that face
+// before the atomics (zpair_flags).
 template <typename T, bool BOX>
 __global__ void __launch_bounds__(256)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    T q[3];
-    load_pos<T, BOX>(src, p, q);
+  const unsigned full = 0xffffffffu;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const int64_t p = base + (threadIdx.x & 31);
+    const bool live = p < n;
+    T q[3] = {T(0), T(0), T(0)};
+    T m = T(0);
+    if (live) {
+      load_pos<T, BOX>(src, p, q);
+      m = mass ? __ldg(mass + p) : mscalar;
+    }
     Corners<T> c;
     cic_corners(q, g, c);
     T lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
-    T m = mass ? __ldg(mass + p) : mscalar;
+    T w[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       int bits = corner_axis_bits(k);
-      T w = mul_rn(corner_weight(lo, hi, bits), m);
-      w = mul_rn(w, corner_ok(c, bits) ? T(1) : T(0));
-      atomicAdd(out + corner_offset(c, bits, g), w);
+      w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
+    }
+    const ZPair zp = zpair_flags(live ? zpair_key(c, g) : kNoPair);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const T t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
+      if (zp.take) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
+    }
+    if (live) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (corner_is_hiz(k) && zp.give) continue;
+        atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
+      }
     }
   }
 }

@@ -163,4 +163,43 @@ __device__ __forceinline__ bool corner_ok(const Corners<T>& c, int bits) {
   return c.ok[0][bits & 1] && c.ok[1][(bits >> 1) & 1] && c.ok[2][(bits >> 2) & 1];
 }
 
+// z-pairing of neighbouring lanes for scatters.  A particle whose stencil does
+// not wrap on any axis gets the key "offset of its lower corner"; others get
+// kNoPair.  If lane i has key K and lane i+1 key K+1, the upper-z face of
+// lane i's stencil (corners 001 101 011 111) is the lower-z face of lane
+// i+1's (000 100 010 110): lane i+1 adds lane i's four values to its own and
+// lane i skips those four atomics.  Particles stored in lattice order pair
+// up along z most of the time, which halves their scatter atomics.
+constexpr uint32_t kNoPair = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ uint32_t zpair_key(const Corners<T>& c, const Grid3& g) {
+  const bool canon = c.o[0][1] == c.o[0][0] + (uint32_t)g.sx && c.o[1][1] == c.o[1][0] + (uint32_t)g.sy &&
+                     c.o[2][1] == c.o[2][0] + 1u;
+  return canon ? c.o[0][0] + c.o[1][0] + c.o[2][0] : kNoPair;
+}
+
+struct ZPair {
+  bool take;  // this lane absorbs the previous lane's upper-z face
+  bool give;  // the next lane absorbs this lane's upper-z face
+};
+
+// Warp-collective (all 32 lanes): pairing flags from each lane's key.
+__device__ __forceinline__ ZPair zpair_flags(uint32_t key) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t kprev = __shfl_up_sync(full, key, 1);
+  ZPair z;
+  z.take = lane > 0 && key != kNoPair && kprev != kNoPair && key == kprev + 1u;
+  const unsigned takers = __ballot_sync(full, z.take);
+  z.give = lane < 31 && ((takers >> (lane + 1)) & 1u);
+  return z;
+}
+
+// Reference corner order k -> axis bits (x = bit 0): the upper-z corners
+// k = 3, 5, 6, 7 pair with the lower-z corners k = 0, 1, 2, 4.
+__device__ __forceinline__ constexpr int zpair_hi(int j) { return j == 0 ? 3 : j == 1 ? 5 : j == 2 ? 6 : 7; }
+__device__ __forceinline__ constexpr int zpair_lo(int j) { return j == 0 ? 0 : j == 1 ? 1 : j == 2 ? 2 : 4; }
+__device__ __forceinline__ constexpr bool corner_is_hiz(int k) { return k == 3 || k >= 5; }
+
 }  // namespace jld

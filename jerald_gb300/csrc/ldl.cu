@@ -12,6 +12,7 @@
 #include "bins.cuh"
 #include "ldl_kernels.cuh"
 #include "ldl_pipe.cuh"
+#include "zpipe.cuh"
 
 namespace jld {
 
@@ -92,6 +93,50 @@ static PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc) {
   p.smem = (size_t)lines * cols * 8 * (2 + nacc) + 64;
   p.ok = true;
   return p;
+}
+
+// Geometry of a pipelined z pass over `nin` meshes (tiles of R whole rows of
+// each), or ok = false when h is not a power of two in [16, 2048] or no even
+// R divides the row count within 512 threads and ~110 KB of shared memory
+// (two CTAs per SM).
+struct ZPipeGeom {
+  bool ok = false;
+  ZTile zt;
+  int nthr = 0;
+  size_t smem = 0;
+};
+
+static ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, bool with_nyq) {
+  ZPipeGeom z;
+  if (h < 16 || h > 2048 || (h & (h - 1))) return z;
+  const int ldw = h + h / 16;
+  for (int R = 32; R >= 2; R >>= 1) {
+    const int lines = nin * R;
+    const int64_t thr = (int64_t)lines * h / 16;
+    const size_t smem = (size_t)lines * h * 8 + (with_nyq ? (size_t)lines * 8 : 0) + (size_t)lines * ldw * 8 + 16;
+    if (thr > 512 || rows % R || smem > 110 * 1024) continue;
+    if (thr < 32) return z;
+    z.ok = true;
+    z.zt.R = R;
+    z.zt.ntiles = (int)(rows / R);
+    z.zt.rows = rows;
+    z.zt.nyq_off = rows * h;
+    z.nthr = (int)thr;
+    z.smem = smem;
+    return z;
+  }
+  return z;
+}
+
+// Persistent grid of a pipelined kernel: every SM full, never more CTAs
+// than tiles.
+template <class K>
+static int persistent_grid(K kern, int nthr, size_t smem, int ntiles, unsigned* grid) {
+  int per_sm = 0;
+  JLD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nthr, smem));
+  if (per_sm < 1) return set_error(JLD_ERR_CUDA, "pipelined z pass does not fit on an SM");
+  *grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)per_sm * sm_count());
+  return JLD_OK;
 }
 
 struct LdlLayout {
@@ -283,6 +328,12 @@ static int ldl_step(const StepArgs& a) {
   const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0), py1 = pipe_geom(nx, ny, h, 1, 1);
   const PipeGeom px1 = pipe_geom(nx, ny, h, 0, 1);
   const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
+  ZPipeGeom zr2c, zc2r3, zadj;
+  if (a.use_pipe) {
+    zr2c = zpipe_geom(rows, h, 1, false);
+    zc2r3 = zpipe_geom(rows, h, 3, true);
+    zadj = zpipe_geom(rows, h, 1, true);
+  }
   // the generic kernels then only cover the nyq plane
   SpecPass gxn = gx.sp, gyn = gy.sp;
   gxn.tiles_main = 0;
@@ -329,7 +380,22 @@ static int ldl_step(const StepArgs& a) {
     float4* g4_l = g4 + (size_t)L.C * l;
     if ((s = paint_into(Xl(l), rho_l))) return s;
     SourcePow src{prm, fact};
-    if ((s = launch_rfft_z_src<float, SourcePow>(st, pl, rho_l, src, W[0], W[0] + nyq_off))) return s;
+    if (zr2c.ok) {
+      s = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zr2c_pipe_kernel<Sch, SourcePow>;
+        unsigned gz = 0;
+        int r = ensure_smem(kern, zr2c.smem);
+        if (!r) r = persistent_grid(kern, zr2c.nthr, zr2c.smem, zr2c.zt.ntiles, &gz);
+        if (r) return r;
+        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(rho_l, src, zr2c.zt, pl.twr, W[0], pl.pz.tw, err);
+        return 0;
+      });
+      if (s) return s;
+      JLD_LAUNCH_CHECK("zr2c_pipe_kernel");
+    } else if ((s = launch_rfft_z_src<float, SourcePow>(st, pl, rho_l, src, W[0], W[0] + nyq_off))) {
+      return s;
+    }
     if ((s = ypass(W[0], -1))) return s;
     if (pipe) {
       CUtensorMap mA;
@@ -379,14 +445,27 @@ static int ldl_step(const StepArgs& a) {
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("yinv3_kernel");
-    s = with_sched(pl.pz, [&](auto sc) {
-      constexpr int SC = decltype(sc)::value;
-      int e = ensure_smem(zinv3_kernel<SC>, 3 * smz);
-      if (e) return e;
-      zinv3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, W[3], W[0], W[4], nyq_off, g4_l, rows,
-                                                       zcols, ilog2i(zcols));
-      return 0;
-    });
+    if (zc2r3.ok) {
+      s = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zc2r3_pipe_kernel<Sch>;
+        unsigned gz = 0;
+        int r = ensure_smem(kern, zc2r3.smem);
+        if (!r) r = persistent_grid(kern, zc2r3.nthr, zc2r3.smem, zc2r3.zt.ntiles, &gz);
+        if (r) return r;
+        kern<<<gz, zc2r3.nthr, zc2r3.smem, st>>>(W[3], W[0], W[4], zc2r3.zt, pl.twr, g4_l, pl.pz.tw, err);
+        return 0;
+      });
+    } else {
+      s = with_sched(pl.pz, [&](auto sc) {
+        constexpr int SC = decltype(sc)::value;
+        int e = ensure_smem(zinv3_kernel<SC>, 3 * smz);
+        if (e) return e;
+        zinv3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, W[3], W[0], W[4], nyq_off, g4_l, rows,
+                                                         zcols, ilog2i(zcols));
+        return 0;
+      });
+    }
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv3_kernel");
     update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
@@ -412,11 +491,21 @@ static int ldl_step(const StepArgs& a) {
     float4* g4_l = g4 + (size_t)L.C * l;
     JLD_CUDA_TRY(cudaMemsetAsync(gb4, 0, sizeof(float4) * L.C, st));
     if (a.binned) {
-      if ((s = ensure_smem(tiled_bwd_kernel, win3))) return s;
-      tiled_bwd_kernel<<<tgrid, 256, win3, st>>>(Xl(l), Xb, tstarts, tg, boxv, cellv, dwv, g, g4_l, gb4, Xb2);
+      if ((s = ensure_smem(tiled_bwd_kernel<true>, win3)) || (s = ensure_smem(tiled_bwd_kernel<false>, win3)))
+        return s;
+      if (l > 0)
+        tiled_bwd_kernel<true><<<tgrid, 256, win3, st>>>(Xl(l), Xb, tstarts, tg, boxv, cellv, dwv, g, g4_l, gb4,
+                                                         Xb2);
+      else
+        tiled_bwd_kernel<false><<<tgrid, 256, win3, st>>>(Xl(l), Xb, tstarts, tg, boxv, cellv, dwv, g, g4_l, gb4,
+                                                          Xb2);
       JLD_LAUNCH_CHECK("tiled_bwd_kernel");
     } else {
-      bwd_particles_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
+      // the first layer's input positions are data: scatter only
+      if (l > 0)
+        bwd_particles_kernel<true><<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
+      else
+        bwd_particles_kernel<false><<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
       JLD_LAUNCH_CHECK("bwd_particles_kernel");
     }
     s = with_sched(pl.pz, [&](auto sc) {
@@ -487,19 +576,35 @@ static int ldl_step(const StepArgs& a) {
     launch_finish(st, part, nparts_x, 4, 1, a.out, 1 + 5 * l, nullptr);
     launch_finish(st, part + 1, nparts_x, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
     if ((s = ypass(W[1], +1))) return s;
-    s = with_sched(pl.pz, [&](auto sc) {
-      constexpr int SC = decltype(sc)::value;
-      int e = ensure_smem(zinv_adj_kernel<SC>, smz);
-      if (e) return e;
-      zinv_adj_kernel<SC><<<zgrid, nthr_z, smz, st>>>(pl.pz, pl.twr, W[1], nyq_off, rho_l, prm, fact, rb, part,
-                                                      rows, zcols, ilog2i(zcols));
-      return 0;
-    });
+    unsigned adj_blocks = zgrid;
+    if (zadj.ok) {
+      s = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zc2r_adj_pipe_kernel<Sch>;
+        int r = ensure_smem(kern, zadj.smem);
+        if (!r) r = persistent_grid(kern, zadj.nthr, zadj.smem, zadj.zt.ntiles, &adj_blocks);
+        if (r) return r;
+        kern<<<adj_blocks, zadj.nthr, zadj.smem, st>>>(W[1], zadj.zt, pl.twr, rho_l, prm, fact,
+                                                       l > 0 ? rb : nullptr, part, pl.pz.tw, err);
+        return 0;
+      });
+    } else {
+      s = with_sched(pl.pz, [&](auto sc) {
+        constexpr int SC = decltype(sc)::value;
+        int e = ensure_smem(zinv_adj_kernel<SC>, smz);
+        if (e) return e;
+        zinv_adj_kernel<SC><<<zgrid, nthr_z, smz, st>>>(pl.pz, pl.twr, W[1], nyq_off, rho_l, prm, fact,
+                                                        l > 0 ? rb : nullptr, part, rows, zcols, ilog2i(zcols));
+        return 0;
+      });
+    }
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv_adj_kernel");
-    launch_finish(st, part, (int)zgrid, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
-    gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
-    JLD_LAUNCH_CHECK("gather_vjp_kernel");
+    launch_finish(st, part, (int)adj_blocks, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
+    if (l > 0) {
+      gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
+      JLD_LAUNCH_CHECK("gather_vjp_kernel");
+    }
     std::swap(Xb, Xb2);
   }
   return JLD_OK;

@@ -409,36 +409,68 @@ update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
 
 // Adjoint of one layer's readout, per particle: Xbar = Xbar' + J^T Xbar'
 // (gather of the float4 force mesh with weight gradients) and the scatter of
-// Xbar' into the float4 cotangent mesh.
+// Xbar' into the float4 cotangent mesh.  GATHER = false (the first layer,
+// whose input positions need no cotangent) does the scatter only.
+template <bool GATHER>
 __global__ void __launch_bounds__(256)
 bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1, int64_t n,
                      BoxGeom bg, Grid3 g, const float4* __restrict__ g4, float4* __restrict__ gb4,
                      float* __restrict__ Xb) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
+  const unsigned full = 0xffffffffu;
+  // warp-uniform grid-stride loop (pairing shuffles); a dead lane re-reads
+  // the last particle with a zero cotangent and stores nothing
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const bool live = base + (threadIdx.x & 31) < n;
+    const int64_t p = live ? base + (threadIdx.x & 31) : n - 1;
     Corners<float> c;
     float lo[3], hi[3];
     particle_setup(X, p, bg, g, c, lo, hi);
-    float v[3] = {__ldg(Xb1 + 3 * p), __ldg(Xb1 + 3 * p + 1), __ldg(Xb1 + 3 * p + 2)};
+    float v[3] = {0.f, 0.f, 0.f};
+    if (live) {
+      v[0] = __ldg(Xb1 + 3 * p); v[1] = __ldg(Xb1 + 3 * p + 1); v[2] = __ldg(Xb1 + 3 * p + 2);
+    }
     float a[3] = {0.f, 0.f, 0.f};
+    float4 s4[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       int bits = corner_axis_bits(k);
-      int64_t off = corner_offset(c, bits, g);
       bool ok = corner_ok(c, bits);
-      float4 gv = __ldg(g4 + off);
-      float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
+      if (GATHER) {
+        float4 gv = __ldg(g4 + corner_offset(c, bits, g));
+        float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
 #pragma unroll
-      for (int e = 0; e < 3; ++e) {
-        float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
-        l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
-        a[e] += ok ? u * wprod(l2, h2, bits) : 0.f;
+        for (int e = 0; e < 3; ++e) {
+          float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
+          l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
+          a[e] += ok ? u * wprod(l2, h2, bits) : 0.f;
+        }
       }
       float w = ok ? wprod(lo, hi, bits) : 0.f;
-      atomicAdd(gb4 + off, make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f));
+      s4[k] = make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f);
     }
+    const ZPair zp = zpair_flags(live ? zpair_key(c, g) : kNoPair);
 #pragma unroll
-    for (int e = 0; e < 3; ++e) Xb[3 * p + e] = v[e] + a[e];
+    for (int jj = 0; jj < 4; ++jj) {
+      const float4 h = s4[zpair_hi(jj)];
+      const float tx = __shfl_up_sync(full, h.x, 1), ty = __shfl_up_sync(full, h.y, 1),
+                  tz = __shfl_up_sync(full, h.z, 1);
+      if (zp.take) {
+        float4& d = s4[zpair_lo(jj)];
+        d.x += tx; d.y += ty; d.z += tz;
+      }
+    }
+    if (live) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (corner_is_hiz(k) && zp.give) continue;
+        atomicAdd(gb4 + corner_offset(c, corner_axis_bits(k), g), s4[k]);
+      }
+      if (GATHER) {
+#pragma unroll
+        for (int e = 0; e < 3; ++e) Xb[3 * p + e] = v[e] + a[e];
+      }
+    }
   }
 }
 
@@ -607,8 +639,9 @@ zinv_adj_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2
         float lb = logf(base);
         float s = powf(base, gamma);
         acc[0].add(cts * s * lb);
-        // base^(gamma-1) = s / base (base > 0)
-        rb[e + q] = cts * gamma * (s / base) * fact;
+        // base^(gamma-1) = s / base (base > 0); rb == nullptr: the first
+        // layer, whose paint cotangent feeds no position cotangent
+        if (rb) rb[e + q] = cts * gamma * (s / base) * fact;
       }
     }
   }

@@ -145,6 +145,28 @@ def test_paint_matches_oracle(jl, dt, nm, box):
     assert np.abs(out.cpu().numpy() - ref2).max() <= _paint_tol(dt, ref2)
 
 
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("nm,box,shift", [((16, 16, 16), (16.0, 16.0, 16.0), 0.0),
+                                          ((12, 10, 18), (24.0, 5.0, 9.0), 0.37)])
+def test_paint_lattice_order(jl, dt, nm, box, shift):
+    # particles in lattice order (z fastest) pair up along z inside a warp;
+    # the last z column wraps, one y row is displaced by a whole cell, the
+    # count is not a multiple of the warp or block size
+    g = np.stack(np.meshgrid(*[np.arange(n) for n in nm], indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+    g[:, 1] += np.where(np.arange(len(g)) % (nm[1] * nm[2]) < nm[2], 1.0, 0.0)
+    cell = np.asarray(box) / np.asarray(nm)
+    pos = ((g + shift + 0.01 * np.sin(np.arange(len(g)))[:, None]) * cell)[:-5].astype(dt)
+    sfx = "f32" if dt == np.float32 else "f64"
+    mass = np.random.default_rng(3).uniform(0.5, 1.5, len(pos)).astype(dt)
+    ref = cic.paint(cic.box_to_mesh(pos, box, nm), mass, nm)
+    out = torch.empty(nm, dtype=torch.float32 if dt == np.float32 else torch.float64, device="cuda")
+    b = _box(box, dt)
+    cscal = ct.c_float(0) if sfx == "f32" else ct.c_double(0)
+    jl.call(f"jld_ppaint_box_{sfx}", _st(), _p(_cuda(pos)), len(pos), _p(_cuda(mass)), cscal, *nm,
+            b.ctypes.data_as(ct.c_void_p), _p(out))
+    assert np.abs(out.cpu().numpy() - ref).max() <= _paint_tol(dt, ref)
+
+
 @pytest.mark.parametrize("method", [0, 1])
 def test_paint_methods_clustered(jl, method):
     # clustered: many particles per cell, signed weights
