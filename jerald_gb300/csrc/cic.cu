@@ -50,18 +50,19 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 
 // ---------------------------------------------------------------------------
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
-// Grid-stride loop a warp at a time (all lanes stay in the loop for the
-// pairing shuffles); lanes whose stencils share a z face merge that face
-// before the atomics (zpair_flags).
+// Warps walk 16 x 2 particle tasks (PairTasks, row-length hint nz; all
+// lanes stay in the loop for the shuffles) and merge the stencil faces
+// their neighbours share before the atomics (pairing_flags).
 template <typename T, bool BOX>
 __global__ void __launch_bounds__(256)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
-    const int64_t p = base + (threadIdx.x & 31);
-    const bool live = p < n;
+  const PairTasks pt(n, g.nz);
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t task = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; task < pt.ntask; task += nw) {
+    const int64_t p = pt.particle(task);
+    const bool live = p >= 0;
     T q[3] = {T(0), T(0), T(0)};
     T m = T(0);
     if (live) {
@@ -79,18 +80,22 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
       int bits = corner_axis_bits(k);
       w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
     }
-    const ZPair zp = zpair_flags(live ? zpair_key(c, g) : kNoPair);
+    const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const T t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
-      if (zp.take) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
+      if (pr.tz) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
+    }
+    {
+      const T t2 = __shfl_up_sync(full, w[2], 16), t4 = __shfl_up_sync(full, w[4], 16);
+      const T t6 = __shfl_up_sync(full, w[6], 16), t7 = __shfl_up_sync(full, w[7], 16);
+      if (pr.ty) { w[0] = add_rn(w[0], t2); w[1] = add_rn(w[1], t4); }
+      if (pr.thz) { w[3] = add_rn(w[3], t6); w[5] = add_rn(w[5], t7); }
     }
     if (live) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        if (corner_is_hiz(k) && zp.give) continue;
-        atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
-      }
+      for (int k = 0; k < 8; ++k)
+        if (pair_keeps(pr, k)) atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
     }
   }
 }

@@ -163,43 +163,84 @@ __device__ __forceinline__ bool corner_ok(const Corners<T>& c, int bits) {
   return c.ok[0][bits & 1] && c.ok[1][(bits >> 1) & 1] && c.ok[2][(bits >> 2) & 1];
 }
 
-// z-pairing of neighbouring lanes for scatters.  A particle whose stencil does
-// not wrap on any axis gets the key "offset of its lower corner"; others get
-// kNoPair.  If lane i has key K and lane i+1 key K+1, the upper-z face of
-// lane i's stencil (corners 001 101 011 111) is the lower-z face of lane
-// i+1's (000 100 010 110): lane i+1 adds lane i's four values to its own and
-// lane i skips those four atomics.  Particles stored in lattice order pair
-// up along z most of the time, which halves their scatter atomics.
+// Pairing of neighbouring particles for scatters.  A warp takes 16
+// consecutive particles of two consecutive "rows" of rl particles (lanes
+// 0-15: p .. p+15, lanes 16-31: the same columns one row later), rl being
+// a hint for the row length of particles stored in lattice order (the mesh
+// z extent).  A particle whose stencil does not wrap on any axis gets the
+// key "offset of its lower corner", others kNoPair.
+//   z pairing: if lane l (l mod 16 > 0) has key K and lane l-1 key K-1, lane
+//   l-1's upper-z face (corners 001 101 011 111) is lane l's lower-z face
+//   (000 100 010 110): lane l adds those four values to its own and lane
+//   l-1 skips their atomics.
+//   y pairing: if lane l >= 16 has key K and lane l-16 key K - sy, the
+//   upper-y corners of lane l-16 still held after z pairing move to lane l:
+//   010 110 always, 011 111 when neither lane gave its upper-z face away.
+// Every value is added by exactly one lane, so the result never depends on
+// the hint or on the pairing rate; particles in lattice order pair most of
+// the time, which removes most of their atomics.
 constexpr uint32_t kNoPair = 0xffffffffu;
 
 template <typename T>
-__device__ __forceinline__ uint32_t zpair_key(const Corners<T>& c, const Grid3& g) {
+__device__ __forceinline__ uint32_t pair_key(const Corners<T>& c, const Grid3& g) {
   const bool canon = c.o[0][1] == c.o[0][0] + (uint32_t)g.sx && c.o[1][1] == c.o[1][0] + (uint32_t)g.sy &&
                      c.o[2][1] == c.o[2][0] + 1u;
   return canon ? c.o[0][0] + c.o[1][0] + c.o[2][0] : kNoPair;
 }
 
-struct ZPair {
-  bool take;  // this lane absorbs the previous lane's upper-z face
-  bool give;  // the next lane absorbs this lane's upper-z face
+struct Pairing {
+  bool tz, gz;    // takes / gives the upper-z face (z pairing)
+  bool ty, gy;    // takes / gives corners 010 110 (y pairing)
+  bool thz, ghz;  // takes / gives corners 011 111 (y pairing of held upper-z corners)
 };
 
-// Warp-collective (all 32 lanes): pairing flags from each lane's key.
-__device__ __forceinline__ ZPair zpair_flags(uint32_t key) {
+// Warp-collective (all 32 lanes, the 16 x 2 layout above).
+__device__ __forceinline__ Pairing pairing_flags(uint32_t key, uint32_t sy) {
   const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const uint32_t kprev = __shfl_up_sync(full, key, 1);
-  ZPair z;
-  z.take = lane > 0 && key != kNoPair && kprev != kNoPair && key == kprev + 1u;
-  const unsigned takers = __ballot_sync(full, z.take);
-  z.give = lane < 31 && ((takers >> (lane + 1)) & 1u);
-  return z;
+  const int lane = threadIdx.x & 31, g = lane & 15;
+  const uint32_t kz = __shfl_up_sync(full, key, 1);
+  const uint32_t ky = __shfl_up_sync(full, key, 16);
+  Pairing p;
+  p.tz = g > 0 && key != kNoPair && kz != kNoPair && key == kz + 1u;
+  const unsigned bz = __ballot_sync(full, p.tz);
+  p.gz = g < 15 && ((bz >> (lane + 1)) & 1u);
+  p.ty = lane >= 16 && key != kNoPair && ky != kNoPair && key == ky + sy;
+  const unsigned bgz = __ballot_sync(full, p.gz);
+  const bool gz_sender = lane >= 16 && ((bgz >> (lane - 16)) & 1u);
+  p.thz = p.ty && !p.gz && !gz_sender;
+  const unsigned by = __ballot_sync(full, p.ty), bh = __ballot_sync(full, p.thz);
+  p.gy = lane < 16 && ((by >> (lane + 16)) & 1u);
+  p.ghz = lane < 16 && ((bh >> (lane + 16)) & 1u);
+  return p;
 }
 
 // Reference corner order k -> axis bits (x = bit 0): the upper-z corners
 // k = 3, 5, 6, 7 pair with the lower-z corners k = 0, 1, 2, 4.
 __device__ __forceinline__ constexpr int zpair_hi(int j) { return j == 0 ? 3 : j == 1 ? 5 : j == 2 ? 6 : 7; }
 __device__ __forceinline__ constexpr int zpair_lo(int j) { return j == 0 ? 0 : j == 1 ? 1 : j == 2 ? 2 : 4; }
-__device__ __forceinline__ constexpr bool corner_is_hiz(int k) { return k == 3 || k >= 5; }
+
+// Whether corner k is still added by this lane after pairing.
+__device__ __forceinline__ bool pair_keeps(const Pairing& p, int k) {
+  if (k == 0 || k == 1) return true;
+  if (k == 2 || k == 4) return !p.gy;
+  if (k == 3 || k == 5) return !p.gz;
+  return !p.gz && !p.ghz;  // k == 6, 7
+}
+
+// Warp task of the 16 x 2 layout: particle index of this lane, or -1.
+struct PairTasks {
+  int64_t n, rl, cpr, ntask;
+  __device__ __forceinline__ PairTasks(int64_t n_, int rl_) : n(n_), rl(rl_) {
+    cpr = (rl + 15) / 16;
+    ntask = ((n + rl - 1) / rl + 1) / 2 * cpr;
+  }
+  __device__ __forceinline__ int64_t particle(int64_t task) const {
+    const int lane = threadIdx.x & 31;
+    const int64_t pr = task / cpr, c = task - pr * cpr;
+    const int64_t col = c * 16 + (lane & 15);
+    const int64_t p = (2 * pr + (lane >> 4)) * rl + col;
+    return (col < rl && p < n) ? p : -1;
+  }
+};
 
 }  // namespace jld

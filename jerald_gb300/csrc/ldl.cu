@@ -106,15 +106,17 @@ struct ZPipeGeom {
   size_t smem = 0;
 };
 
-static ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, bool with_nyq) {
+// slot_row = staging bytes per row of the tile (all meshes), cap = shared
+// memory limit.
+static ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, size_t slot_row, size_t cap = 110 * 1024) {
   ZPipeGeom z;
   if (h < 16 || h > 2048 || (h & (h - 1))) return z;
   const int ldw = h + h / 16;
   for (int R = 32; R >= 2; R >>= 1) {
     const int lines = nin * R;
     const int64_t thr = (int64_t)lines * h / 16;
-    const size_t smem = (size_t)lines * h * 8 + (with_nyq ? (size_t)lines * 8 : 0) + (size_t)lines * ldw * 8 + 16;
-    if (thr > 512 || rows % R || smem > 110 * 1024) continue;
+    const size_t smem = (size_t)R * slot_row + (size_t)lines * ldw * 8 + 16;
+    if (thr > 512 || rows % R || smem > cap) continue;
     if (thr < 32) return z;
     z.ok = true;
     z.zt.R = R;
@@ -328,11 +330,12 @@ static int ldl_step(const StepArgs& a) {
   const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0), py1 = pipe_geom(nx, ny, h, 1, 1);
   const PipeGeom px1 = pipe_geom(nx, ny, h, 0, 1);
   const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
-  ZPipeGeom zr2c, zc2r3, zadj;
+  ZPipeGeom zr2c, zc2r3, zadj, zr2c3;
   if (a.use_pipe) {
-    zr2c = zpipe_geom(rows, h, 1, false);
-    zc2r3 = zpipe_geom(rows, h, 3, true);
-    zadj = zpipe_geom(rows, h, 1, true);
+    zr2c = zpipe_geom(rows, h, 1, (size_t)h * 8);
+    zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8);
+    zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8);
+    zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16, 120 * 1024);
   }
   // the generic kernels then only cover the nyq plane
   SpecPass gxn = gx.sp, gyn = gy.sp;
@@ -508,14 +511,27 @@ static int ldl_step(const StepArgs& a) {
         bwd_particles_kernel<false><<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
       JLD_LAUNCH_CHECK("bwd_particles_kernel");
     }
-    s = with_sched(pl.pz, [&](auto sc) {
-      constexpr int SC = decltype(sc)::value;
-      int e = ensure_smem(zfwd3_kernel<SC>, 3 * smz);
-      if (e) return e;
-      zfwd3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, kt.cz, gb4, W[0], W[1], W[2], nyq_off,
-                                                       rows, zcols, ilog2i(zcols));
-      return 0;
-    });
+    if (zr2c3.ok) {
+      s = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zr2c3_pipe_kernel<Sch>;
+        unsigned gz = 0;
+        int r = ensure_smem(kern, zr2c3.smem);
+        if (!r) r = persistent_grid(kern, zr2c3.nthr, zr2c3.smem, zr2c3.zt.ntiles, &gz);
+        if (r) return r;
+        kern<<<gz, zr2c3.nthr, zr2c3.smem, st>>>(gb4, zr2c3.zt, pl.twr, kt.cz, W[0], W[1], W[2], pl.pz.tw, err);
+        return 0;
+      });
+    } else {
+      s = with_sched(pl.pz, [&](auto sc) {
+        constexpr int SC = decltype(sc)::value;
+        int e = ensure_smem(zfwd3_kernel<SC>, 3 * smz);
+        if (e) return e;
+        zfwd3_kernel<SC><<<zgrid, nthr_z, 3 * smz, st>>>(pl.pz, pl.twr, kt.cz, gb4, W[0], W[1], W[2], nyq_off,
+                                                         rows, zcols, ilog2i(zcols));
+        return 0;
+      });
+    }
     if (s) return s;
     JLD_LAUNCH_CHECK("zfwd3_kernel");
     if (pipe) {

@@ -203,13 +203,23 @@ __device__ __forceinline__ void spec_columns(const SpecPass& sp, int ax, int64_t
 // ---------------------------------------------------------------------------
 // Forward kernels.
 
+// base^e for base > 0 as exp2(e * log2(base)), optionally with ln(base):
+// one logarithm and one exponential instead of powf's extended-precision
+// path.  Relative error: a few ulp plus |e * log2(base)| * 2^-24, far
+// inside the FP32 tolerance of the step.
+__device__ __forceinline__ float pow_pos(float base, float e, float* ln_base = nullptr) {
+  const float l2 = log2f(base);
+  if (ln_base) *ln_base = l2 * 0.693147180559945f;
+  return exp2f(e * l2);
+}
+
 struct SourcePow {
   const float* params;  // gamma at params[1]
   float fact;
   __device__ __forceinline__ float operator()(float v, int64_t) const {
     float gamma = __ldg(params + 1);
     float rho = __fmul_rn(v, fact);
-    return powf(__fadd_rn(rho, 1e-8f), gamma);
+    return pow_pos(__fadd_rn(rho, 1e-8f), gamma);
   }
 };
 
@@ -417,12 +427,14 @@ bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1,
                      BoxGeom bg, Grid3 g, const float4* __restrict__ g4, float4* __restrict__ gb4,
                      float* __restrict__ Xb) {
   const unsigned full = 0xffffffffu;
-  // warp-uniform grid-stride loop (pairing shuffles); a dead lane re-reads
-  // the last particle with a zero cotangent and stores nothing
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
-    const bool live = base + (threadIdx.x & 31) < n;
-    const int64_t p = live ? base + (threadIdx.x & 31) : n - 1;
+  // warp tasks of the 16 x 2 pairing layout (row-length hint nz); a dead
+  // lane re-reads the last particle with a zero cotangent and stores nothing
+  const PairTasks pt(n, g.nz);
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t task = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; task < pt.ntask; task += nw) {
+    const int64_t pp = pt.particle(task);
+    const bool live = pp >= 0;
+    const int64_t p = live ? pp : n - 1;
     Corners<float> c;
     float lo[3], hi[3];
     particle_setup(X, p, bg, g, c, lo, hi);
@@ -449,23 +461,26 @@ bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1,
       float w = ok ? wprod(lo, hi, bits) : 0.f;
       s4[k] = make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f);
     }
-    const ZPair zp = zpair_flags(live ? zpair_key(c, g) : kNoPair);
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      const float4 h = s4[zpair_hi(jj)];
-      const float tx = __shfl_up_sync(full, h.x, 1), ty = __shfl_up_sync(full, h.y, 1),
-                  tz = __shfl_up_sync(full, h.z, 1);
-      if (zp.take) {
-        float4& d = s4[zpair_lo(jj)];
+    const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
+    auto move = [&](int from, int to, int delta, bool take) {
+      const float4 h = s4[from];
+      const float tx = __shfl_up_sync(full, h.x, delta), ty = __shfl_up_sync(full, h.y, delta),
+                  tz = __shfl_up_sync(full, h.z, delta);
+      if (take) {
+        float4& d = s4[to];
         d.x += tx; d.y += ty; d.z += tz;
       }
-    }
+    };
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) move(zpair_hi(jj), zpair_lo(jj), 1, pr.tz);
+    move(2, 0, 16, pr.ty);
+    move(4, 1, 16, pr.ty);
+    move(6, 3, 16, pr.thz);
+    move(7, 5, 16, pr.thz);
     if (live) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        if (corner_is_hiz(k) && zp.give) continue;
-        atomicAdd(gb4 + corner_offset(c, corner_axis_bits(k), g), s4[k]);
-      }
+      for (int k = 0; k < 8; ++k)
+        if (pair_keeps(pr, k)) atomicAdd(gb4 + corner_offset(c, corner_axis_bits(k), g), s4[k]);
       if (GATHER) {
 #pragma unroll
         for (int e = 0; e < 3; ++e) Xb[3 * p + e] = v[e] + a[e];
@@ -571,10 +586,10 @@ loss_kernel(const float* __restrict__ rho_paint, const float* __restrict__ targe
        e += (int64_t)gridDim.x * blockDim.x) {
     float rho = __fmul_rn(__ldg(rho_paint + e), fact);
     float m = mask ? __ldg(mask + e) : 1.f;
-    float F, base = 0.f, pw = 0.f, u = 0.f;
+    float F, base = 0.f, pw = 0.f, u = 0.f, lnb = 0.f;
     if (kind == 0) {
       base = __fadd_rn(rho, 1e-8f);
-      pw = powf(base, mu);
+      pw = pow_pos(base, mu, &lnb);
       u = __fadd_rn(__fmul_rn(w, pw), b);
       F = u > 1e-12f ? u : 1e-12f;
     } else {
@@ -588,7 +603,7 @@ loss_kernel(const float* __restrict__ rho_paint, const float* __restrict__ targe
     float r;
     if (kind == 0) {
       float ctu = u > 1e-12f ? ctF : 0.f;
-      acc[1].add(ctu * w * pw * logf(base));
+      acc[1].add(ctu * w * pw * lnb);
       acc[2].add(ctu * pw);
       acc[3].add(ctu);
       // base^(mu-1) = pw / base (base > 0)
@@ -636,8 +651,8 @@ zinv_adj_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2
         float cts = q ? z.y : z.x;
         float rho = __fmul_rn(__ldg(rho_paint + e + q), fact);
         float base = __fadd_rn(rho, 1e-8f);
-        float lb = logf(base);
-        float s = powf(base, gamma);
+        float lb;
+        float s = pow_pos(base, gamma, &lb);
         acc[0].add(cts * s * lb);
         // base^(gamma-1) = s / base (base > 0); rb == nullptr: the first
         // layer, whose paint cotangent feeds no position cotangent

@@ -76,14 +76,6 @@ __device__ __forceinline__ float2 c2r_pack_tile(const float2* slot, const float2
   return make_float2(a.x - t.y, a.y + t.x);
 }
 
-// Shared-memory layout of a z pass: staging slot, work buffer, mbarrier.
-template <class Sch>
-struct ZSmem {
-  static size_t bytes(int lines, int slot_elems) {
-    return (size_t)slot_elems * 8 + (size_t)lines * ZShape<Sch>::LDW * 8 + 16;
-  }
-};
-
 // Number of tiles of this CTA (grid-stride over tiles).
 __device__ __forceinline__ int z_my_tiles(int ntiles) {
   return (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -284,8 +276,8 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
         const float cts = q ? z.y : z.x;
         const float rho = __fmul_rn(q ? rp.y : rp.x, fact);
         const float base = __fadd_rn(rho, 1e-8f);
-        const float lb = logf(base);
-        const float s = powf(base, gamma);
+        float lb;
+        const float s = pow_pos(base, gamma, &lb);
         acc[0].add(cts * s * lb);
         o[q] = cts * gamma * (s / base) * fact;
       }
@@ -294,6 +286,83 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
     __syncthreads();
   }
   block_reduce_kahan<1>(acc, partials, 1);
+}
+
+// ---------------------------------------------------------------------------
+// First adjoint z pass: r2c of the three cotangent channels of the float4
+// mesh gb4 (rows of 2h float4) into Ax, Ay and c_z(kz) * Az (main + nyq).
+// Lines 0..R-1 of a tile are channel x, R..2R-1 channel y, 2R..3R-1 z; all
+// three read the same staged float4 rows.
+template <class Sch>
+__global__ void __launch_bounds__(512)
+zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __restrict__ twr,
+                  const float* __restrict__ cz, float2* __restrict__ Ax, float2* __restrict__ Ay,
+                  float2* __restrict__ Az, const float2* __restrict__ tw, int* err) {
+  using Z = ZShape<Sch>;
+  constexpr int H = Z::H;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const int R = zt.R;
+  float4* slot = reinterpret_cast<float4*>(smraw);
+  float2* work = reinterpret_cast<float2*>(slot + R * 2 * H);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(work + 3 * R * Z::LDW);
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+  __syncthreads();
+  const uint32_t bytes = (uint32_t)R * 2 * H * 16u;
+  const int ntl = z_my_tiles(zt.ntiles);
+  auto issue = [&](int t) {
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_load_1d(slot, gb4 + (int64_t)t * R * 2 * H, bytes, bar);
+  };
+  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  RowWork<Z::PSH> wk{work, Z::LDW};
+  float2* dst[3] = {Ax, Ay, Az};
+  for (int i = 0; i < ntl; ++i) {
+    const int t = blockIdx.x + i * gridDim.x;
+    const bool more = i + 1 < ntl;
+    const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0 && err) atomicExch(err, 9);
+      return;
+    }
+    auto in0 = [&](int c, int j) {
+      const int d = c / R, r = c - d * R;
+      const float4 a = slot[r * 2 * H + 2 * j], b = slot[r * 2 * H + 2 * j + 1];
+      return d == 0 ? make_float2(a.x, b.x) : d == 1 ? make_float2(a.y, b.y) : make_float2(a.z, b.z);
+    };
+    auto rel = [&]() {
+      if (tid == 0 && more) {
+        fence_proxy_async_smem();
+        issue(t + gridDim.x);
+      }
+    };
+    p2_rows_to_work<Sch>(wk, in0, rel, tw, -1, tid, nthr);
+    __syncthreads();
+    constexpr int HH = H / 2 + 1;
+    const int64_t row0 = (int64_t)t * R;
+    for (int f = tid; f < 3 * R * HH; f += nthr) {
+      const int c = f / HH, k = f - c * HH;
+      const int d = c / R, r = c - d * R;
+      const int64_t row = row0 + r;
+      const float2 z = wk.at(c, k & (H - 1));
+      const float2 zm = wk.at(c, (H - k) & (H - 1));
+      const float2 zc = make_float2(zm.x, -zm.y);
+      const float2 xe = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+      const float2 dd = make_float2(0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y));
+      const float2 xo = make_float2(dd.y, -dd.x);
+      const float2 w = __ldg(twr + k);
+      const float2 wxo = make_float2(w.x * xo.x - w.y * xo.y, w.x * xo.y + w.y * xo.x);
+      const float2 xk = make_float2(xe.x + wxo.x, xe.y + wxo.y);
+      const float2 xhk = make_float2(xe.x - wxo.x, -(xe.y - wxo.y));
+      const float s1 = d == 2 ? __ldg(cz + k) : 1.f;
+      const float s2 = d == 2 ? __ldg(cz + (H - k)) : 1.f;
+      float2* o = dst[d];
+      o[row * H + k] = make_float2(xk.x * s1, xk.y * s1);
+      if (k == 0) o[zt.nyq_off + row] = make_float2(xhk.x * s2, xhk.y * s2);
+      else if (H - k != k) o[row * H + (H - k)] = make_float2(xhk.x * s2, xhk.y * s2);
+    }
+    __syncthreads();
+  }
 }
 
 }  // namespace jld
