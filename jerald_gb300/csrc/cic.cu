@@ -53,8 +53,10 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 // Warps walk 16 x 2 particle tasks (PairTasks, row-length hint nz; all
 // lanes stay in the loop for the shuffles) and merge the stencil faces
 // their neighbours share before the atomics (pairing_flags).
+// Occupancy matters more than registers here (latency-bound loads and
+// atomics): six CTAs of 256 threads per SM in single precision.
 template <typename T, bool BOX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;

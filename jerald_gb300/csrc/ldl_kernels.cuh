@@ -394,7 +394,7 @@ __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int
 
 // X' = X + readout of the float4 force mesh (three channels, the reference's
 // per-channel summation order).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
 update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
               const float4* __restrict__ g4, float* __restrict__ Xn) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
@@ -422,7 +422,7 @@ update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
 // Xbar' into the float4 cotangent mesh.  GATHER = false (the first layer,
 // whose input positions need no cotangent) does the scatter only.
 template <bool GATHER>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1, int64_t n,
                      BoxGeom bg, Grid3 g, const float4* __restrict__ g4, float4* __restrict__ gb4,
                      float* __restrict__ Xb) {
