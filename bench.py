@@ -116,17 +116,28 @@ def make_workload(n: int, device, seed: int = 0):
     return pos.contiguous(), box
 
 
-def make_target(pos, n, box, params, device):
+def make_target(pos, n, box, params, device, nstep: int = 2):
+    """The model's own output times lognormal noise (sigma 0.1); above 512^3
+    (where the plain primitive path would need several times the fused
+    step's memory) the noise field alone."""
     import torch
     from jerald_gb300 import synth
+    noise = torch.from_numpy(synth.lognormal_noise((n, n, n), 0.1, seed=2).astype(np.float32)).to(device)
+    if n > 512:
+        return noise.contiguous()
     from jerald_gb300.model import JERALDModel
     from jerald_gb300.pmesh import PMesh
     pm = PMesh(n, box, device=device, dtype=torch.float32)
-    model = JERALDModel(pos, None, pm, Nstep=2, kind="sm")
+    model = JERALDModel(pos, None, pm, Nstep=nstep, kind="sm")
     with torch.no_grad():
-        F = model.evaluate(torch.as_tensor(params, dtype=torch.float32, device=device), pos, 2)
-    noise = torch.from_numpy(synth.lognormal_noise(F.shape, 0.1, seed=2).astype(np.float32)).to(device)
+        F = model.evaluate(torch.as_tensor(params, dtype=torch.float32, device=device), pos, nstep)
     return (F * noise).contiguous()
+
+
+def yardstick_bytes(N: int, nstep: int) -> int:
+    """Plain-primitive byte yardstick of one fwd+adjoint step (N = C): per
+    layer 108N forward and 224N adjoint, 16N final paint, 48N its adjoint."""
+    return (332 * nstep + 64) * N
 
 
 def time_primitives(pos, n, box, steps, warmup):
@@ -172,11 +183,15 @@ def time_primitives(pos, n, box, steps, warmup):
     return res
 
 
-def count_launches(nstep: int, kind: str, mask: bool) -> int:
-    fwd = 7 * nstep
-    final = 1 + (1 if mask else 0) + 1 + 1 + (2 if kind == "sm" else 1) + 1
-    bwd = 9 * nstep
-    return fwd + final + bwd
+def count_launches(nstep: int, kind: str, mask: bool, recompute: bool = False) -> int:
+    """Kernel launches of one fused step on a power-of-two mesh with the
+    pipelined passes (used only when the captured graph cannot be asked)."""
+    force_mesh = 8                      # z r2c, y pass (2), x filter (2), inverse y (2), inverse z
+    fwd = nstep * (1 + force_mesh + 1)  # paint, force mesh, update
+    final = 1 + 1 + (2 if kind == "sm" else 1) + 1 + (1 if mask else 0)
+    adj = nstep * 12 + (nstep - 1)      # + position cotangent gathers of layers >= 1
+    rec = force_mesh * max(0, nstep - 2) if recompute else 0
+    return 1 + fwd + final + adj + rec
 
 
 def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int | None = None):
@@ -307,6 +322,9 @@ def main():
     ap.add_argument("--precision", action="store_true",
                     help="compare the fused FP32 step with the FP64 primitive pipeline on the workload")
     ap.add_argument("--paint", default="atomic", choices=["atomic", "warp", "tiled"])
+    ap.add_argument("--nstep", type=int, default=2, help="displacement layers")
+    ap.add_argument("--recompute", action="store_true",
+                    help="memory plan: one force-mesh slot, recomputed in the adjoint")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -318,9 +336,8 @@ def main():
         return run_precision(args)
 
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from jerald_gb300 import replicas
+    world, rank, local = replicas.world()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if world > 1:
@@ -332,15 +349,16 @@ def main():
     from jerald_gb300 import synth
     from jerald_gb300.ldl import FusedLDL
 
-    n = args.n
-    params = synth.default_params(2)
-    pos, box = make_workload(n, dev, seed=rank)
-    target = make_target(pos, n, box, params, dev)
+    n, nstep = args.n, args.nstep
+    params = synth.default_params(nstep)
+    pos, box = make_workload(n, dev, seed=replicas.replica_seed(rank))
+    target = make_target(pos, n, box, params, dev, nstep)
     N = pos.shape[0]
-    step = FusedLDL(n, box, N, nstep=2, kind="sm", L1=True, grad_mode="reference", paint_method=args.paint,
-                    device=dev)
+    step = FusedLDL(n, box, N, nstep=nstep, kind="sm", L1=True, grad_mode="reference", paint_method=args.paint,
+                    device=dev, recompute=args.recompute)
     step(pos, params, target)
     step.capture(pos, target)
+    launches_per_step = step.graph_kernels()
     for _ in range(args.warmup):
         step.replay(params)
     torch.cuda.synchronize()
@@ -359,13 +377,9 @@ def main():
             step.replay(params)
         e1.record(st)
         barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+    value, ms = replicas.aggregate_rate(e0.elapsed_time(e1) / args.steps, dev)
     loss, grad = step.out[0].item(), step.out[1:].cpu().numpy()
+    assert step.error_word() == 0, "a pipelined pass gave up waiting for a copy"
 
     # e2e: host buffers -> device, step, loss+grads -> host
     pos_h = pos.cpu().pin_memory()
@@ -388,11 +402,8 @@ def main():
         out_h.copy_(step.out, non_blocking=True)
     e3.record(st)
     barrier()
-    ms_e2e = e2.elapsed_time(e3) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    e2e_value, ms_e2e = replicas.aggregate_rate(e2.elapsed_time(e3) / args.steps, dev)
+    del pos_h, tgt_h
 
     extra = {}
     peak, peak_kind = _peaks()
@@ -406,11 +417,11 @@ def main():
                 "kernel": dominant, "peak_kind": peak_kind,
                 "kernels": {k: {"gbs": v["gbs"], "frac": v["gbs"] / peak, "ms": v["ms"]} for k, v in kern.items()}}
 
-    if not args.no_plain and rank == 0:
+    if not args.no_plain and rank == 0 and n <= 512:
         from jerald_gb300.model import JERALDModel
         from jerald_gb300.pmesh import PMesh
         pm = PMesh(n, box, device=dev, dtype=torch.float32)
-        model = JERALDModel(pos, target, pm, Nstep=2, kind="sm")
+        model = JERALDModel(pos, target, pm, Nstep=nstep, kind="sm")
         pt = torch.as_tensor(params, dtype=torch.float32)
         lp, gp = model.loss_and_grad(pt)
         torch.cuda.synchronize()
@@ -437,19 +448,25 @@ def main():
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
+    ysb = yardstick_bytes(N, nstep)
+    extra["yardstick"] = {"bytes_per_step": ysb, "gbs": ysb / ms / 1e6, "frac": ysb / ms / 1e6 / peak,
+                          "note": "plain-primitive byte yardstick (332*nstep+64)*N over the fused step time"}
+    extra["workspace_gb"] = step.workspace_bytes / 1e9
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Zel'dovich lattice + Gaussian halos)",
-                "config": {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, 2 sm layers + "
-                                       f"ReLU map, L1 loss, fwd+adjoint (13 grads), graph-captured",
-                           "nmesh": n, "nparts": N, "box": box, "nstep": 2, "kind": "sm",
-                           "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1
+                "config": {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, {nstep} sm layers + "
+                                       f"ReLU map, L1 loss, fwd+adjoint ({5 * nstep + 3} grads), graph-captured",
+                           "nmesh": n, "nparts": N, "box": box, "nstep": nstep, "kind": "sm",
+                           "memory_plan": "recompute force meshes" if args.recompute else "checkpoint",
+                           "l2": "inputs larger than L2 (no flush)", "parallelism": f"{world} replicas" if world > 1
                            else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu,
-                "e2e": {"value": world * 1000.0 / ms_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
-                "gpu_launches": count_launches(2, "sm", False) * args.steps,
+                "gpu_launches": (launches_per_step if launches_per_step is not None
+                                 else count_launches(nstep, "sm", False, args.recompute)) * args.steps,
                 "clocks": clk.summary(), "loss": loss, **extra}
         print(json.dumps(line), flush=True)
     if world > 1:

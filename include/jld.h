@@ -65,6 +65,10 @@ enum {
 JLD_API const char* jld_version(void);
 JLD_API const char* jld_status_string(int status);
 JLD_API const char* jld_last_error(void);
+/* Number of kernel nodes in a captured CUDA graph (cudaGraph_t passed as */
+/* void*): the kernel launches one replay issues.  No counterpart in the  */
+/* reference (measurement helper).                                        */
+JLD_API int jld_graph_kernel_nodes(void* graph, int64_t* kernels);
 
 /* ------------------------------------------------------------------ */
 /* Layout bookkeeping.                                                  */
@@ -241,12 +245,23 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /*           bit 1: generic pass kernels instead of the TMA-pipelined ones */
 /*           bit 2: bin the particles into 16^3-cell tiles first (counting */
 /*                  sort) and scatter through shared-memory tile windows   */
+/*           bit 3: memory plan for large boxes: one force-mesh slot; the  */
+/*                  adjoint recomputes the force meshes of layers          */
+/*                  1 .. nstep-2 from their stored densities (one extra    */
+/*                  spectral forward per such layer) instead of keeping    */
+/*                  nstep-1 slots of 16 bytes per cell                      */
 /*   out     device float64: [loss, d loss / d params ...]                 */
 /* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
 /* into a CUDA graph; parameters are read from device memory, so a graph  */
 /* replays with whatever `params` holds.                                  */
+/* Workspace bytes for the given option bits (0 for invalid arguments);    */
+/* jld_ldl_workspace_f32 is the size for options = 4, enough for any      */
+/* option set without bit 3.  No counterpart in the reference (its        */
+/* buffers are library globals, lib/cpu.cc:15-25).                        */
 JLD_API size_t jld_ldl_workspace_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
                                      int32_t nstep);
+JLD_API size_t jld_ldl_workspace_opt_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                                         int32_t nstep, int32_t options);
 JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float box[3]);
 JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts,
                              int32_t nx, int32_t ny, int32_t nz, const float box[3],

@@ -62,6 +62,7 @@ _SIGS = {
     "jld_ldl_positions_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _i32, _c_void_p],
     "jld_ldl_error_word_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
     "jld_ldl_order_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
+    "jld_graph_kernel_nodes": [_c_void_p, _c_void_p],
 }
 _RESTYPES = {
     "jld_version": ct.c_char_p,
@@ -70,9 +71,11 @@ _RESTYPES = {
     "jld_fft_workspace_f32": _size,
     "jld_fft_workspace_f64": _size,
     "jld_ldl_workspace_f32": _size,
+    "jld_ldl_workspace_opt_f32": _size,
 }
 _EXTRA_ARGS = {
     "jld_ldl_workspace_f32": [_i32, _i32, _i32, _i64, _i32],
+    "jld_ldl_workspace_opt_f32": [_i32, _i32, _i32, _i64, _i32, _i32],
     "jld_status_string": [ct.c_int],
     "jld_fft_workspace_f32": [_i32, _i32, _i32],
     "jld_fft_workspace_f64": [_i32, _i32, _i32],

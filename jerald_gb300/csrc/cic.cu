@@ -50,7 +50,7 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 
 // ---------------------------------------------------------------------------
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
-// Warps walk 16 x 2 particle tasks (PairTasks, row-length hint nz; all
+// Warps walk 16 x 2 particle tasks (PairWalk, row-length hint nz; all
 // lanes stay in the loop for the shuffles) and merge the stencil faces
 // their neighbours share before the atomics (pairing_flags).
 // Occupancy matters more than registers here (latency-bound loads and
@@ -60,10 +60,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;
-  const PairTasks pt(n, g.nz);
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t task = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; task < pt.ntask; task += nw) {
-    const int64_t p = pt.particle(task);
+  for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
+    const int64_t p = pw.particle();
     const bool live = p >= 0;
     T q[3] = {T(0), T(0), T(0)};
     T m = T(0);

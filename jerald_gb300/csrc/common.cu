@@ -1,6 +1,8 @@
 // Status strings, the thread-local error message and the stateless layout
 // entry points (initLayout / clean of lib/cpu.cc:29-49).
 
+#include <vector>
+
 #include "common.cuh"
 
 #include <string.h>
@@ -87,6 +89,24 @@ int jld_init_layout(int32_t commsize, int32_t lyidx) {
                           commsize);
   if (lyidx < 0 || lyidx > 4)
     return jld::set_error(JLD_ERR_ARG, "initLayout: lyidx needs to be between 0 and 4");
+  return JLD_OK;
+}
+
+// Kernel nodes of a captured CUDA graph (the launches one replay issues).
+int jld_graph_kernel_nodes(void* graph, int64_t* kernels) {
+  jld::clear_error();
+  if (!graph || !kernels) return jld::set_error(JLD_ERR_ARG, "jld_graph_kernel_nodes: NULL argument");
+  size_t n = 0;
+  JLD_CUDA_TRY(cudaGraphGetNodes((cudaGraph_t)graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n) JLD_CUDA_TRY(cudaGraphGetNodes((cudaGraph_t)graph, nodes.data(), &n));
+  int64_t k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    JLD_CUDA_TRY(cudaGraphNodeGetType(nodes[i], &t));
+    if (t == cudaGraphNodeTypeKernel) ++k;
+  }
+  *kernels = k;
   return JLD_OK;
 }
 

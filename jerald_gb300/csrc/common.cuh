@@ -227,16 +227,32 @@ __device__ __forceinline__ bool pair_keeps(const Pairing& p, int k) {
   return !p.gz && !p.ghz;  // k == 6, 7
 }
 
-// Warp task of the 16 x 2 layout: particle index of this lane, or -1.
-struct PairTasks {
-  int64_t n, rl, cpr, ntask;
-  __device__ __forceinline__ PairTasks(int64_t n_, int rl_) : n(n_), rl(rl_) {
+// Warp walk over the tasks of the 16 x 2 layout (grid-stride over tasks;
+// the task -> (row pair, 16-column chunk) split is advanced incrementally,
+// without a 64-bit division per iteration).
+struct PairWalk {
+  int64_t n, rl, cpr, ntask, nw, spr, sc;  // sizes; per-iteration stride in (row pair, chunk)
+  int64_t task, pr, c;                     // current task and its (row pair, chunk)
+  __device__ __forceinline__ PairWalk(int64_t n_, int rl_) : n(n_), rl(rl_) {
     cpr = (rl + 15) / 16;
     ntask = ((n + rl - 1) / rl + 1) / 2 * cpr;
+    nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    spr = nw / cpr;
+    sc = nw - spr * cpr;
+    task = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    pr = task / cpr;
+    c = task - pr * cpr;
   }
-  __device__ __forceinline__ int64_t particle(int64_t task) const {
+  __device__ __forceinline__ bool more() const { return task < ntask; }
+  __device__ __forceinline__ void next() {
+    task += nw;
+    pr += spr;
+    c += sc;
+    if (c >= cpr) { c -= cpr; ++pr; }
+  }
+  // particle index of this lane in the current task, or -1
+  __device__ __forceinline__ int64_t particle() const {
     const int lane = threadIdx.x & 31;
-    const int64_t pr = task / cpr, c = task - pr * cpr;
     const int64_t col = c * 16 + (lane & 15);
     const int64_t p = (2 * pr + (lane >> 4)) * rl + col;
     return (col < rl && p < n) ? p : -1;

@@ -145,7 +145,7 @@ struct LdlLayout {
   int64_t N, C, H;
   int nstep;
   size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
-      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, total;
+      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, off_g4x, total;
   TileGeom tg;
   int64_t part_doubles;
 };
@@ -154,7 +154,25 @@ static size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
 static constexpr int kMaxCellBlocks = 8192;
 static constexpr int kTileCells = 16;  // binning tile edge (cells)
 
-static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
+// Option bits of the fused step (jld_ldl_step_f32).
+constexpr int kOptWarpPaint = 1;   // warp-aggregated paint atomics
+constexpr int kOptGeneric = 2;     // generic (non-pipelined) FFT passes
+constexpr int kOptBinned = 4;      // per-step binning, tile-privatized scatters
+constexpr int kOptRecompute = 8;   // one force-mesh slot, recomputed in the adjoint
+constexpr int kOptAll = 15;
+
+// Force-mesh slots: the adjoint reads layer l's force mesh for l >= 1 only
+// (the first layer's input positions need no cotangent), so nstep - 1 slots
+// hold every mesh it needs; with kOptRecompute one slot, and the adjoint
+// recomputes layers 1 .. nstep-2 from their stored density.
+static int g4_slots(int nstep, int options) {
+  return (options & kOptRecompute) ? 1 : std::max(1, nstep - 1);
+}
+
+// Workspace layout.  Everything up to the error word is independent of the
+// options, then the binning buffers (kOptBinned), then the extra force-mesh
+// slots.
+static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep, int options) {
   LdlLayout L;
   const int64_t h = nz / 2;
   L.N = N; L.nstep = nstep;
@@ -168,7 +186,7 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
   L.off_xb2 = o; o += al(sizeof(float) * 3 * N);               // (pong)
   L.off_rho = o; o += al(sizeof(float) * L.C * (nstep + 1));   // unit-mass paint per layer + final
   L.off_S = o; o += al(sizeof(float2) * L.H * nstep);          // FFT of the source per layer
-  L.off_g4 = o; o += al(sizeof(float4) * L.C * nstep);         // force mesh per layer
+  L.off_g4 = o; o += al(sizeof(float4) * L.C);                 // force mesh, slot 0
   for (int i = 0; i < 5; ++i) { L.off_w[i] = o; o += al(sizeof(float2) * L.H); }
   L.off_gb4 = o; o += al(sizeof(float4) * L.C);                // 3-channel cotangent mesh
   L.off_rb = o; o += al(sizeof(float) * L.C);                  // density cotangent
@@ -177,10 +195,14 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep) {
   L.off_err = o; o += al(sizeof(int) * 4);                     // pipelined-pass error word
   // particle binning: tile-ordered X_0, tile keys, order, tile counts/starts/fill
   L.tg = make_tile_geom(nx, ny, nz, kTileCells, 1);
-  L.off_xs0 = o; o += al(sizeof(float) * 3 * N);
-  L.off_keys = o; o += al(sizeof(int) * N);
-  L.off_perm = o; o += al(sizeof(int) * N);
-  L.off_tiles = o; o += al(sizeof(int) * (3 * (size_t)L.tg.ntiles() + 1));
+  L.off_xs0 = L.off_keys = L.off_perm = L.off_tiles = 0;
+  if (options & kOptBinned) {
+    L.off_xs0 = o; o += al(sizeof(float) * 3 * N);
+    L.off_keys = o; o += al(sizeof(int) * N);
+    L.off_perm = o; o += al(sizeof(int) * N);
+    L.off_tiles = o; o += al(sizeof(int) * (3 * (size_t)L.tg.ntiles() + 1));
+  }
+  L.off_g4x = o; o += al(sizeof(float4) * L.C * (g4_slots(nstep, options) - 1));  // slots 1 ..
   L.total = o;
   return L;
 }
@@ -192,6 +214,7 @@ struct StepArgs {
   int nstep, kind, L1, mode, paint_method;
   bool use_pipe;         // TMA-pipelined strided passes where the mesh qualifies
   bool binned;           // particles binned into tiles; tile-privatized scatters
+  int options;           // option bits (layout)
   const float* params;   // device: 5*nstep (+3 for kind 0)
   const float* target; const float* mask;
   char* ws;
@@ -229,7 +252,8 @@ static void launch_finish(cudaStream_t st, const double* part, int nblocks, int 
 
 static int ldl_step(const StepArgs& a) {
   const int nx = a.nx, ny = a.ny, nz = a.nz, h = nz / 2;
-  const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep);
+  const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep, a.options);
+  const bool recompute = (a.options & kOptRecompute) != 0;
   cudaStream_t st = a.st;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   JLD_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
@@ -256,6 +280,12 @@ static int ldl_step(const StepArgs& a) {
   float* rho = (float*)(ws + L.off_rho);
   float2* Sbuf = (float2*)(ws + L.off_S);
   float4* g4 = (float4*)(ws + L.off_g4);
+  float4* g4x = (float4*)(ws + L.off_g4x);
+  // force-mesh slot of layer l (g4_slots)
+  auto g4_of = [&](int l) -> float4* {
+    const int sl = (recompute || l == 0) ? 0 : l - 1;
+    return sl == 0 ? g4 : g4x + (size_t)L.C * (sl - 1);
+  };
   float2* W[5];
   for (int i = 0; i < 5; ++i) W[i] = (float2*)(ws + L.off_w[i]);
   float4* gb4 = (float4*)(ws + L.off_gb4);
@@ -375,13 +405,14 @@ static int ldl_step(const StepArgs& a) {
     return launch_line_pass<float>(st, pl.py, jn, none, sgn);
   };
 
-  // ---------------- forward layers
-  for (int l = 0; l < a.nstep; ++l) {
+  // Force mesh of layer l from its stored unit-mass density: source map and
+  // r2c along z, y FFT, x FFT (S_l) with the filter and gradient factors,
+  // inverse y of three channels, inverse z into the float4 mesh g4_l.
+  auto force_mesh = [&](int l, float4* g4_l) -> int {
+    int s = JLD_OK;
     const float* prm = a.params + 5 * l;
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
-    float4* g4_l = g4 + (size_t)L.C * l;
-    if ((s = paint_into(Xl(l), rho_l))) return s;
     SourcePow src{prm, fact};
     if (zr2c.ok) {
       s = with_p2(h, [&](auto sch) {
@@ -471,6 +502,14 @@ static int ldl_step(const StepArgs& a) {
     }
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv3_kernel");
+    return JLD_OK;
+  };
+
+  // ---------------- forward layers
+  for (int l = 0; l < a.nstep; ++l) {
+    float4* g4_l = g4_of(l);
+    if ((s = paint_into(Xl(l), rho + (size_t)L.C * l))) return s;
+    if ((s = force_mesh(l, g4_l))) return s;
     update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
     JLD_LAUNCH_CHECK("update_kernel");
   }
@@ -491,7 +530,9 @@ static int ldl_step(const StepArgs& a) {
     const float* prm = a.params + 5 * l;
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
-    float4* g4_l = g4 + (size_t)L.C * l;
+    float4* g4_l = g4_of(l);
+    // the last layer's mesh is still in its slot; layer 0's is not read
+    if (recompute && l > 0 && l < a.nstep - 1 && (s = force_mesh(l, g4_l))) return s;
     JLD_CUDA_TRY(cudaMemsetAsync(gb4, 0, sizeof(float4) * L.C, st));
     if (a.binned) {
       if ((s = ensure_smem(tiled_bwd_kernel<true>, win3)) || (s = ensure_smem(tiled_bwd_kernel<false>, win3)))
@@ -647,7 +688,13 @@ extern "C" {
 
 JLD_API size_t jld_ldl_workspace_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts, int32_t nstep) {
   if (nx < 1 || ny < 1 || nz < 2 || nparts < 1 || nstep < 1) return 0;
-  return ldl_layout(nx, ny, nz, nparts, nstep).total;
+  return ldl_layout(nx, ny, nz, nparts, nstep, kOptBinned).total;
+}
+
+JLD_API size_t jld_ldl_workspace_opt_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts, int32_t nstep,
+                                         int32_t options) {
+  if (nx < 1 || ny < 1 || nz < 2 || nparts < 1 || nstep < 1 || (options & ~kOptAll)) return 0;
+  return ldl_layout(nx, ny, nz, nparts, nstep, options).total;
 }
 
 JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float box[3]) {
@@ -673,12 +720,12 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
   if (grad_mode != 0 && grad_mode != 1)
     return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
-  if (options & ~7) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
-  if ((options & 4) && nparts > INT32_MAX)
+  if (options & ~kOptAll) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
+  if ((options & kOptBinned) && nparts > INT32_MAX)
     return set_error(JLD_ERR_UNSUPPORTED, "%s: binning needs fewer than 2^31 particles", who);
   const int paint_method = options & 1;
   if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
-  size_t need = ldl_layout(nx, ny, nz, nparts, nstep).total;
+  size_t need = ldl_layout(nx, ny, nz, nparts, nstep, options).total;
   if (!ws || ws_bytes < need)
     return set_error(JLD_ERR_WORKSPACE, "%s: workspace of %zu bytes needed, got %zu", who, need,
                      ws ? ws_bytes : (size_t)0);
@@ -688,8 +735,9 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   a.nx = nx; a.ny = ny; a.nz = nz;
   for (int i = 0; i < 3; ++i) a.box[i] = box[i];
   a.nstep = nstep; a.kind = kind; a.L1 = L1; a.mode = grad_mode; a.paint_method = paint_method;
-  a.use_pipe = (options & 2) == 0;
-  a.binned = (options & 4) != 0;
+  a.use_pipe = (options & kOptGeneric) == 0;
+  a.binned = (options & kOptBinned) != 0;
+  a.options = options;
   a.params = params; a.target = target; a.mask = mask;
   a.ws = (char*)ws; a.out = out;
   return ldl_step(a);
@@ -699,7 +747,7 @@ JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32
                                    int32_t nstep, const int** out) {
   clear_error();
   if (!ws || !out || nstep < 1 || nparts < 1) return set_error(JLD_ERR_ARG, "jld_ldl_error_word_f32: bad arguments");
-  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep, 0);  // base offsets do not depend on options
   *out = (const int*)((const char*)ws + L.off_err);
   return JLD_OK;
 }
@@ -708,7 +756,7 @@ JLD_API int jld_ldl_order_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz
                               int32_t nstep, const int** out) {
   clear_error();
   if (!ws || !out || nstep < 1 || nparts < 1) return set_error(JLD_ERR_ARG, "jld_ldl_order_f32: bad arguments");
-  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep, kOptBinned);
   *out = (const int*)((const char*)ws + L.off_perm);
   return JLD_OK;
 }
@@ -718,7 +766,7 @@ JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_
   clear_error();
   if (!ws || !out || layer < 1 || layer > nstep)
     return set_error(JLD_ERR_ARG, "jld_ldl_positions_f32: bad arguments");
-  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep);
+  LdlLayout L = ldl_layout(nx, ny, nz, nparts, nstep, 0);
   *out = (const float*)((const char*)ws + L.off_pos) + (size_t)3 * nparts * (layer - 1);
   return JLD_OK;
 }

@@ -429,10 +429,8 @@ bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1,
   const unsigned full = 0xffffffffu;
   // warp tasks of the 16 x 2 pairing layout (row-length hint nz); a dead
   // lane re-reads the last particle with a zero cotangent and stores nothing
-  const PairTasks pt(n, g.nz);
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t task = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; task < pt.ntask; task += nw) {
-    const int64_t pp = pt.particle(task);
+  for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
+    const int64_t pp = pw.particle();
     const bool live = pp >= 0;
     const int64_t p = live ? pp : n - 1;
     Corners<float> c;

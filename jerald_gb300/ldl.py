@@ -30,7 +30,7 @@ _PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
                  grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
-                 pipelined: bool = True):
+                 pipelined: bool = True, recompute: bool = False):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
         self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
@@ -41,12 +41,13 @@ class FusedLDL:
         self.grad_mode = grad_mode
         self.paint_method = paint_method
         self.pipelined = bool(pipelined)
+        self.recompute = bool(recompute)
         self.nparts = int(nparts)
         self.nstep = int(nstep)
         self.nparams = 5 * self.nstep + (3 if kind == "sm" else 0)
         self.device = torch.device(device)
         lib = _lib.load()
-        nbytes = lib.jld_ldl_workspace_f32(*self.nmesh, self.nparts, self.nstep)
+        nbytes = lib.jld_ldl_workspace_opt_f32(*self.nmesh, self.nparts, self.nstep, self.options)
         if nbytes == 0:
             raise ValueError("invalid fused-step geometry")
         self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
@@ -56,6 +57,11 @@ class FusedLDL:
             _lib.call("jld_ldl_prepare_f32", *self.nmesh, self.box.ctypes.data_as(ct.c_void_p))
         self.graph = None
         self._static = None
+
+    @property
+    def options(self) -> int:
+        """Option bits of jld_ldl_step_f32."""
+        return _PAINT[self.paint_method] | (0 if self.pipelined else 2) | (8 if self.recompute else 0)
 
     @property
     def workspace_bytes(self) -> int:
@@ -71,7 +77,7 @@ class FusedLDL:
         st = ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         _lib.call("jld_ldl_step_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
                   self.box.ctypes.data_as(ct.c_void_p), self.nstep, _KINDS[self.kind], int(self.L1),
-                  _MODES[self.grad_mode], _PAINT[self.paint_method] | (0 if self.pipelined else 2),
+                  _MODES[self.grad_mode], self.options,
                   ct.c_void_p(self.params.data_ptr()),
                   ct.c_void_p(target.data_ptr()), ct.c_void_p(mask.data_ptr()) if mask is not None else None,
                   ct.c_void_p(self.ws.data_ptr()), self.ws.numel(), ct.c_void_p(self.out.data_ptr()))
@@ -108,6 +114,15 @@ class FusedLDL:
             self._set_params(params)
         self.graph.replay()
         return self.out[0], self.out[1:]
+
+    def graph_kernels(self):
+        """Kernel launches one replay of the captured graph issues (None
+        before capture or when torch does not expose the raw graph)."""
+        if self.graph is None or not hasattr(self.graph, "raw_cuda_graph"):
+            return None
+        k = ct.c_int64(0)
+        _lib.call("jld_graph_kernel_nodes", ct.c_void_p(self.graph.raw_cuda_graph()), ct.byref(k))
+        return int(k.value)
 
     def error_word(self) -> int:
         """Nonzero if a pipelined pass of the last step gave up waiting for a copy."""

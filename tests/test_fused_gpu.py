@@ -60,6 +60,34 @@ def test_fused_matches_fp64_oracle(kind, L1, mask, mode):
     assert _rel(g, g_o).max() < 1e-2
 
 
+@pytest.mark.parametrize("recompute", [False, True])
+def test_fused_three_layers_memory_plans(recompute):
+    # nstep = 3: the adjoint needs the force meshes of layers 1 and 2; with
+    # recompute they share one slot and layer 1's is rebuilt from its density
+    n, box = 32, 100.0
+    X, p, tgt, o, _ = _case(n, box, "sm", True, 31, nstep=3)
+    p = np.concatenate([synth_params3(), p[-3:]])
+    loss_o, g_o = o.loss_and_grad(p, X, tgt.astype(np.float64), 3, mode="true")
+    from jerald_gb300.ldl import FusedLDL
+    f = FusedLDL(n, box, len(X), nstep=3, kind="sm", L1=True, grad_mode="true", recompute=recompute)
+    pos = torch.from_numpy(X.astype(np.float32)).cuda()
+    loss, g = f(pos, p, torch.from_numpy(tgt).cuda())
+    torch.cuda.synchronize()
+    assert f.error_word() == 0
+    assert abs(float(loss) - loss_o) <= 1e-5 * abs(loss_o)
+    g = g.cpu().numpy()
+    assert np.linalg.norm(g - g_o) / np.linalg.norm(g_o) < 1e-3
+    assert _rel(g, g_o).max() < 1e-2
+    if recompute:
+        full = FusedLDL(n, box, len(X), nstep=3, kind="sm", L1=True, grad_mode="true")
+        assert f.workspace_bytes < full.workspace_bytes
+
+
+def synth_params3():
+    # three layers with different strengths (alpha, gamma, kh, kl, nu)
+    return np.array([0.05, 1.0, 0.5, 2.0, 1.0, 0.04, 0.9, 0.6, 1.8, 1.1, 0.03, 1.1, 0.5, 2.2, 0.9])
+
+
 def test_fused_positions_match_oracle_layers():
     n, box = 32, 100.0
     X, p, tgt, o, _ = _case(n, box, "sm", True, 5)
