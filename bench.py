@@ -268,6 +268,54 @@ def run_profile(args):
     return 0
 
 
+def run_batch(args):
+    """Many independent boxes (meshes 64..256^3, one particle per cell,
+    parameters within +-50% of the 64^3 configuration's) autotuned and
+    captured into one CUDA graph; boxes/s and particle-steps/s."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300.batch import FusedLDLBatch, make_c3_boxes
+    dev = torch.device("cuda", 0)
+    boxes, params = make_c3_boxes(seed=0, nbox=args.batch, device=dev)
+    b = FusedLDLBatch(boxes, streams=4, tune=True, device=dev)
+    b.capture()
+    for _ in range(args.warmup):
+        b.replay(params)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        b.replay(params)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # the same boxes one after another, each as its own graph (no branches)
+    serial = 0.0
+    for bx, p in zip(boxes, params):
+        one = FusedLDLBatch([bx], streams=1, tune=False, device=dev)
+        one.capture()
+        for _ in range(args.warmup):
+            one.replay([p])
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            one.replay([p])
+        e1.record(st)
+        torch.cuda.synchronize()
+        serial += e0.elapsed_time(e1) / args.steps
+        del one
+    npart = sum(int(bx.pos.shape[0]) for bx in boxes)
+    print(json.dumps({"workload": f"{len(boxes)} boxes, meshes {sorted(int(bx.nmesh) for bx in boxes)}, "
+                                  f"one particle per cell, 2 sm layers, one graph",
+                      "ms_per_batch": ms, "boxes_per_s": len(boxes) * 1000.0 / ms,
+                      "particle_steps_per_s": npart * 1000.0 / ms, "serial_graphs_ms": serial,
+                      "graph_kernels": b.graph_kernels(),
+                      "configs": [bx.config for bx in boxes]}), flush=True)
+    return 0
+
+
 def run_precision(args):
     """Fused FP32 step vs the FP64 primitive pipeline (plain JERALDModel in
     float64 on the same positions and target): loss and gradient errors."""
@@ -323,6 +371,8 @@ def main():
                     help="compare the fused FP32 step with the FP64 primitive pipeline on the workload")
     ap.add_argument("--paint", default="atomic", choices=["atomic", "warp", "tiled"])
     ap.add_argument("--nstep", type=int, default=2, help="displacement layers")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="instead of the main workload: N boxes of mixed meshes in one graph (prints its own line)")
     ap.add_argument("--recompute", action="store_true",
                     help="memory plan: one force-mesh slot, recomputed in the adjoint")
     args = ap.parse_args()
@@ -334,6 +384,8 @@ def main():
         return run_profile(args)
     if args.precision:
         return run_precision(args)
+    if args.batch:
+        return run_batch(args)
 
     import torch
     from jerald_gb300 import replicas

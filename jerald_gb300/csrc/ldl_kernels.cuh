@@ -102,23 +102,24 @@ struct Green {
 };
 __device__ __forceinline__ Green green_fn(float kx, float ky, float kz, int kind, float kh,
                                           float kl, float nu) {
+  // G = -exp(E) k^nu = -2^(E log2(e) + nu log2(k)): one logarithm and one
+  // exponential per mode
+  constexpr float kLog2e = 1.4426950408889634f, kLn2 = 0.6931471805599453f;
   float k = sqrtf(kx * kx + ky * ky + kz * kz);
   if (k == 0.f) k = 1e-8f;
   Green r;
-  float lk = logf(k);
+  const float l2k = log2f(k);
   if (kind == 1) {  // dm
-    float e = expf(-k / kl - kh / k);
-    r.g = -e * expf(nu * lk);
+    r.g = -exp2f((-k / kl - kh / k) * kLog2e + nu * l2k);
     r.dkh = r.g * (-1.f / k);
     r.dkl = r.g * (k / (kl * kl));
   } else {          // sm
-    float k2 = k * k;
-    float e = expf(-k2 / (kl * kl) - kh * kh / k2);
-    r.g = -e * expf(nu * lk);
+    const float k2 = k * k;
+    r.g = -exp2f((-k2 / (kl * kl) - kh * kh / k2) * kLog2e + nu * l2k);
     r.dkh = r.g * (-2.f * kh / k2);
     r.dkl = r.g * (2.f * k2 / (kl * kl * kl));
   }
-  r.dnu = r.g * lk;
+  r.dnu = r.g * (l2k * kLn2);
   return r;
 }
 

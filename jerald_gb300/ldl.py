@@ -27,6 +27,25 @@ _MODES = {"reference": 0, "true": 1}
 _PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 
 
+def _new_graph():
+    """A CUDA graph whose cudaGraph_t stays queryable after instantiation
+    (for counting its kernel nodes) where torch supports that."""
+    try:
+        g = torch.cuda.CUDAGraph(keep_graph=True)
+        g._jld_kept = True
+    except TypeError:
+        g = torch.cuda.CUDAGraph()
+        g._jld_kept = False
+    return g
+
+
+def _finish_capture(g) -> None:
+    """Instantiates a kept graph right after capture (a graph that is not
+    kept was instantiated by the capture itself)."""
+    if getattr(g, "_jld_kept", False):
+        g.instantiate()
+
+
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
                  grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
@@ -102,9 +121,10 @@ class FusedLDL:
         with torch.cuda.stream(s):
             self._launch(pos, target, mask)  # builds plans, tables and kernel attributes
         torch.cuda.current_stream(self.device).wait_stream(s)
-        self.graph = torch.cuda.CUDAGraph()
+        self.graph = _new_graph()
         with torch.cuda.graph(self.graph):
             self._launch(pos, target, mask)
+        _finish_capture(self.graph)
         return self.graph
 
     def replay(self, params=None):
@@ -120,8 +140,12 @@ class FusedLDL:
         before capture or when torch does not expose the raw graph)."""
         if self.graph is None or not hasattr(self.graph, "raw_cuda_graph"):
             return None
+        try:
+            raw = self.graph.raw_cuda_graph()
+        except RuntimeError:  # graph not kept after instantiation
+            return None
         k = ct.c_int64(0)
-        _lib.call("jld_graph_kernel_nodes", ct.c_void_p(self.graph.raw_cuda_graph()), ct.byref(k))
+        _lib.call("jld_graph_kernel_nodes", ct.c_void_p(raw), ct.byref(k))
         return int(k.value)
 
     def error_word(self) -> int:
