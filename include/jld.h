@@ -183,6 +183,10 @@ JLD_API int jld_buildplan_f32(int32_t nx, int32_t ny, int32_t nz, int32_t local_
 JLD_API int jld_buildplan_f64(int32_t nx, int32_t ny, int32_t nz, int32_t local_out[2]);
 
 /* Workspace bytes the FFT entry points need (Nx*Ny*(Nz/2+1) complex).  */
+/* Single-precision calls on power-of-two meshes (16 <= Nx, Ny, Nz/2 <=  */
+/* 2048) run the TMA-pipelined passes when the input, workspace and       */
+/* output are 16-byte aligned (8 for an interleaved r2c output), and the  */
+/* generic passes otherwise; both give the same transform.                */
 JLD_API size_t jld_fft_workspace_f32(int32_t nx, int32_t ny, int32_t nz);
 JLD_API size_t jld_fft_workspace_f64(int32_t nx, int32_t ny, int32_t nz);
 
@@ -234,6 +238,7 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /* model.py:351-403, its gradient through value_and_grad at 410-413), for  */
 /* kind 0 = "sm" (potential_gradient_sm, model.py:186-212, ReLU bias map   */
 /* model.py:338-344) and kind 1 = "dm" (model.py:137-179, 346-347).        */
+/* The workspace must be 256-byte aligned (cudaMalloc'd memory is).        */
 /*   pos     (nparts, 3) float32 box-unit positions (device)               */
 /*   params  device float32: 5 per layer (alpha, gamma, kh, kl, nu),      */
 /*           then (mu, w, b) for kind 0                                    */
@@ -254,6 +259,12 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
 /* into a CUDA graph; parameters are read from device memory, so a graph  */
 /* replays with whatever `params` holds.                                  */
+/* Error word of the pipelined single-precision FFT passes on the current */
+/* device, read after a device synchronisation (0 = fine; nonzero = a pass */
+/* gave up waiting for a tile copy and stopped early, so some output since */
+/* the last reset is invalid); reset != 0 clears it.  No counterpart in    */
+/* the reference.                                                          */
+JLD_API int jld_fft_pipe_status(int32_t* value, int32_t reset);
 /* Workspace bytes for the given option bits (0 for invalid arguments);    */
 /* jld_ldl_workspace_f32 is the size for options = 4, enough for any      */
 /* option set without bit 3.  No counterpart in the reference (its        */

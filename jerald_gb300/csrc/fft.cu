@@ -22,9 +22,11 @@
 #include <tuple>
 #include <vector>
 #include <cmath>
+#include <type_traits>
 
 #include "fft_core.cuh"
 #include "fft_passes.cuh"
+#include "pipe_host.cuh"
 
 namespace jld {
 
@@ -188,6 +190,141 @@ static int fft_args_check(int nx, int ny, int nz, const void* ws, size_t ws_byte
   return JLD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined single-precision transforms for power-of-two meshes
+// (16 <= nx, ny, nz/2 <= 2048): the z pass and the y pass run on the
+// TMA / bulk-copy staged kernels of the fused step, the x pass of the r2c
+// writes the caller's layout straight from its last FFT stage.  The nyq
+// plane (kz = nz/2) keeps the generic line kernel.  The c2r reads the
+// caller's layout with the generic x pass (its rows of nz/2+1 complex values
+// are not 16-byte aligned for a tensor copy) and pipelines y and z.
+//
+// A copy that never arrives makes a pipelined pass stop after a bounded wait
+// and set the library's pass error word (jld_fft_error_word).
+static __device__ int g_fft_pipe_err;
+static std::mutex g_err_mu;
+static int* g_err_ptr[64];
+
+static int fft_err_word(int** out) {
+  int dev = 0;
+  JLD_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(JLD_ERR_UNSUPPORTED, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_err_mu);
+  if (!g_err_ptr[dev]) JLD_CUDA_TRY(cudaGetSymbolAddress((void**)&g_err_ptr[dev], g_fft_pipe_err));
+  *out = g_err_ptr[dev];
+  return JLD_OK;
+}
+
+static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+struct FftPipe {
+  bool ok = false;
+  PipeGeom py, px;
+  ZPipeGeom z;
+};
+
+static FftPipe fft_pipe_geom(int nx, int ny, int nz, bool c2r) {
+  FftPipe f;
+  const int h = nz / 2;
+  const int64_t rows = (int64_t)nx * ny;
+  f.py = pipe_geom(nx, ny, h, 1, 0);
+  f.px = pipe_geom(nx, ny, h, 0, 0);
+  f.z = c2r ? zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8) : zpipe_geom(rows, h, 1, (size_t)h * 8);
+  f.ok = f.py.ok && f.px.ok && f.z.ok && (c2r || f.px.ok);
+  return f;
+}
+
+// y FFT of the internal layout in place: pipelined main block + nyq rows.
+static int pipe_y_pass(cudaStream_t st, const Plan3<float>& pl, const FftPipe& fp, float2* main, int sgn,
+                       int* err) {
+  const int nx = pl.nx, ny = pl.ny, h = pl.h;
+  CUtensorMap m;
+  int s = make_main_map(&m, main, nx, ny, h, 1, fp.py.g.cols, ny);
+  if (s) return s;
+  s = with_p2(ny, [&](auto sch) {
+    using Sch = decltype(sch);
+    auto kern = sgn < 0 ? spass_kernel<Sch, 1, -1> : spass_kernel<Sch, 1, 1>;
+    int r = ensure_smem(kern, fp.py.smem);
+    if (r) return r;
+    kern<<<fp.py.grid, fp.py.nthr, fp.py.smem, st>>>(m, main, fp.py.g, pl.py.tw, err);
+    return 0;
+  });
+  if (s) return s;
+  JLD_LAUNCH_CHECK("spass_kernel");
+  LineJob<float> jn, none;
+  float2* nq = main + (size_t)nx * ny * h;
+  jn.src = nq; jn.dst = nq;
+  jn.es_in = jn.es_out = 1;
+  jn.cdiv_in = jn.cdiv_out = 1;
+  jn.cmul_in = jn.cmul_out = ny;
+  jn.ncol = nx;
+  return launch_line_pass<float>(st, pl.py, jn, none, sgn);
+}
+
+static int rfft3_pipe(cudaStream_t st, const Plan3<float>& pl, const FftPipe& fp, const float* data,
+                      float2* out_c, float* out_re, float* out_im, float2* main) {
+  const int nx = pl.nx, ny = pl.ny, h = pl.h;
+  int* err = nullptr;
+  int s = fft_err_word(&err);
+  if (s) return s;
+  s = with_p2(h, [&](auto sch) {
+    using Sch = decltype(sch);
+    auto kern = zr2c_pipe_kernel<Sch, SrcIdentity>;
+    unsigned gz = 0;
+    int r = ensure_smem(kern, fp.z.smem);
+    if (!r) r = persistent_grid(kern, fp.z.nthr, fp.z.smem, fp.z.zt.ntiles, &gz);
+    if (r) return r;
+    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(data, SrcIdentity{}, fp.z.zt, pl.twr, main, pl.pz.tw, err);
+    return 0;
+  });
+  if (s) return s;
+  JLD_LAUNCH_CHECK("zr2c_pipe_kernel");
+  if ((s = pipe_y_pass(st, pl, fp, main, -1, err))) return s;
+  CUtensorMap m;
+  if ((s = make_main_map(&m, main, nx, ny, h, 0, fp.px.g.cols, nx))) return s;
+  s = with_p2(nx, [&](auto sch) {
+    using Sch = decltype(sch);
+    auto kern = xref_pipe_kernel<Sch, -1>;
+    int r = ensure_smem(kern, fp.px.smem);
+    if (r) return r;
+    kern<<<fp.px.grid, fp.px.nthr, fp.px.smem, st>>>(m, out_c, out_re, out_im, fp.px.g, pl.px.tw, err);
+    return 0;
+  });
+  if (s) return s;
+  JLD_LAUNCH_CHECK("xref_pipe_kernel");
+  LineJob<float> jn = job_x_internal<float>(pl, main + (size_t)nx * ny * h, true), none;
+  set_job_out_ref<float>(jn, pl, true, out_c, out_re, out_im);
+  return launch_line_pass<float>(st, pl.px, jn, none, -1);
+}
+
+static int irfft3_pipe(cudaStream_t st, const Plan3<float>& pl, const FftPipe& fp, const float2* in_c,
+                       const float* in_re, const float* in_im, float* out, float2* main) {
+  const int nx = pl.nx, ny = pl.ny, h = pl.h;
+  int* err = nullptr;
+  int s = fft_err_word(&err);
+  if (s) return s;
+  float2* nyq = main + (size_t)nx * ny * h;
+  LineJob<float> jm = job_x_internal<float>(pl, main, false);
+  LineJob<float> jn = job_x_internal<float>(pl, nyq, true);
+  set_job_in_ref<float>(jm, pl, false, in_c, in_re, in_im);
+  set_job_in_ref<float>(jn, pl, true, in_c, in_re, in_im);
+  if ((s = launch_line_pass<float>(st, pl.px, jm, jn, +1))) return s;
+  if ((s = pipe_y_pass(st, pl, fp, main, +1, err))) return s;
+  s = with_p2(h, [&](auto sch) {
+    using Sch = decltype(sch);
+    auto kern = zc2r_pipe_kernel<Sch>;
+    unsigned gz = 0;
+    int r = ensure_smem(kern, fp.z.smem);
+    if (!r) r = persistent_grid(kern, fp.z.nthr, fp.z.smem, fp.z.zt.ntiles, &gz);
+    if (r) return r;
+    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(main, fp.z.zt, pl.twr, out, pl.pz.tw, err);
+    return 0;
+  });
+  if (s) return s;
+  JLD_LAUNCH_CHECK("zc2r_pipe_kernel");
+  return JLD_OK;
+}
+
 // r2c: data (nx,ny,nz) real -> out in caller layout (interleaved, or split
 // when out_c == nullptr).
 template <typename T>
@@ -202,6 +339,12 @@ static int rfft3(cudaStream_t st, const T* data, int nx, int ny, int nz, cplx_t<
   const int h = pl.h;
   cplx_t<T>* main = (cplx_t<T>*)ws;
   cplx_t<T>* nyq = main + (size_t)nx * ny * h;
+  if constexpr (std::is_same<T, float>::value) {
+    // bulk and tensor copies need 16-byte aligned sources and staging
+    const bool aligned = al16(data) && al16(ws) && ((uintptr_t)out_c % 8 == 0);
+    const FftPipe fp = fft_pipe_geom(nx, ny, nz, false);
+    if (fp.ok && aligned) return rfft3_pipe(st, pl, fp, data, out_c, out_re, out_im, main);
+  }
   if ((s = launch_rfft_z<T>(st, pl, data, nullptr, main, nyq))) return s;
   if ((s = launch_y_pass<T>(st, pl, main, nyq, -1))) return s;
   // x pass: internal -> caller layout (row length h+1)
@@ -224,6 +367,11 @@ static int irfft3(cudaStream_t st, const cplx_t<T>* in_c, const T* in_re, const 
   const int h = pl.h;
   cplx_t<T>* main = (cplx_t<T>*)ws;
   cplx_t<T>* nyq = main + (size_t)nx * ny * h;
+  if constexpr (std::is_same<T, float>::value) {
+    const bool aligned = al16(ws) && al16(out);
+    const FftPipe fp = fft_pipe_geom(nx, ny, nz, true);
+    if (fp.ok && aligned) return irfft3_pipe(st, pl, fp, in_c, in_re, in_im, out, main);
+  }
   LineJob<T> jm = job_x_internal<T>(pl, main, false);
   LineJob<T> jn = job_x_internal<T>(pl, nyq, true);
   set_job_in_ref<T>(jm, pl, false, in_c, in_re, in_im);
@@ -422,6 +570,18 @@ int jld_pfft_c_static_f32(jld_stream_t s, const float* data, int32_t nx, int32_t
                           void* out) {
   clear_error();
   return pfft_static_impl(ST(s), data, nx, ny, nz, (float2*)out);
+}
+
+JLD_API int jld_fft_pipe_status(int32_t* value, int32_t reset) {
+  clear_error();
+  if (!value) return set_error(JLD_ERR_ARG, "jld_fft_pipe_status: NULL argument");
+  int* p = nullptr;
+  int s = fft_err_word(&p);
+  if (s) return s;
+  JLD_CUDA_TRY(cudaDeviceSynchronize());
+  JLD_CUDA_TRY(cudaMemcpy(value, p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (reset) JLD_CUDA_TRY(cudaMemset(p, 0, sizeof(int32_t)));
+  return JLD_OK;
 }
 
 }  // extern "C"

@@ -113,3 +113,60 @@ spass_kernel(const __grid_constant__ CUtensorMap m_in, float2* out, SGeom g, con
 }
 
 }  // namespace jld
+
+namespace jld {
+
+// ---------------------------------------------------------------------------
+// x pass (AX 0) of the main block with the result written in the caller's
+// half-spectrum layout (nx, ny, h+1): interleaved complex (out_c) or split
+// real / imaginary arrays (out_re, out_im).  A tile's columns are `cols`
+// consecutive kz of one y (cols divides h), so each line's stores are one
+// contiguous run.
+template <class Sch, int SGN>
+__global__ void __launch_bounds__(512)
+xref_pipe_kernel(const __grid_constant__ CUtensorMap m_in, float2* __restrict__ out_c, float* __restrict__ out_re,
+                 float* __restrict__ out_im, SGeom g, const float2* __restrict__ tw, int* err) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int tile_elems = g.lines * g.cols;
+  PipeSmem s = pipe_smem(smraw, tile_elems, 1, 0);
+  if (tid == 0) {
+    mbar_init(s.bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  if (tid == 0 && ntl > 0) issue_tile<0>(&m_in, s.slot[0], s.bar, g, blockIdx.x);
+  ColWork wk{s.work, g.cols};
+  const int64_t row = (int64_t)g.ny * (g.h + 1);  // caller-layout stride between x lines
+  for (int i = 0; i < ntl; ++i) {
+    const int t = blockIdx.x + i * gridDim.x;
+    bool ok = mbar_wait_bounded(s.bar, (uint32_t)(i & 1));
+    if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 11); return; }
+    const float2* slot = s.slot[0];
+    const int64_t col0 = (int64_t)t << g.cshift;  // (y, kz) column index y * h + kz
+    const int64_t y = col0 / g.h, kz0 = col0 - y * g.h;
+    const int64_t o0 = y * (g.h + 1) + kz0;
+    const bool more = i + 1 < ntl;
+    auto in = [&](int c, int j) { return slot[j * g.cols + c]; };
+    auto st = [&](int c, int j, float2 v) {
+      const int64_t o = o0 + c + (int64_t)j * row;
+      if (out_c) {
+        out_c[o] = v;
+      } else {
+        out_re[o] = v.x;
+        out_im[o] = v.y;
+      }
+    };
+    auto release = [&]() {
+      if (tid == 0 && more) {
+        fence_proxy_async_smem();
+        issue_tile<0>(&m_in, s.slot[0], s.bar, g, t + gridDim.x);
+      }
+    };
+    p2_run_rel<Sch, true>(wk, in, st, release, tw, SGN, g.cshift, tid, nthr);
+    __syncthreads();
+  }
+}
+
+}  // namespace jld

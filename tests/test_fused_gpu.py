@@ -185,6 +185,29 @@ def test_pipelined_passes_match_generic_passes(n):
     assert float((xa - xb).abs().max()) < 1e-4
 
 
+@pytest.mark.parametrize("nm", [(512, 16, 32), (16, 512, 64), (64, 32, 1024)])
+def test_pipelined_passes_match_generic_non_cubic(nm):
+    # long x / y / z lines: narrower pipelined tiles (two CTAs per SM) and
+    # few rows per z tile
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    rng = np.random.default_rng(23)
+    box = np.asarray(nm, dtype=np.float64) * 1.5
+    N = int(np.prod(nm))
+    X = (rng.uniform(0, 1, (N, 3)) * box).astype(np.float32)
+    pos = torch.from_numpy(X).cuda()
+    t = torch.from_numpy(synth.lognormal_noise(nm, 0.1, seed=3).astype(np.float32)).cuda()
+    p = synth.default_params(2)
+    fa = FusedLDL(nm, box, N, nstep=2, kind="sm", L1=False, grad_mode="true")
+    fb = FusedLDL(nm, box, N, nstep=2, kind="sm", L1=False, grad_mode="true", pipelined=False)
+    la, ga = [v.clone() for v in fa(pos, p, t)]
+    lb, gb = [v.clone() for v in fb(pos, p, t)]
+    torch.cuda.synchronize()
+    assert fa.error_word() == 0
+    assert abs(float(la) - float(lb)) <= 1e-6 * abs(float(lb))
+    assert _rel(ga.cpu().numpy(), gb.cpu().numpy()).max() < 1e-3
+
+
 def test_fused_rejects_bad_arguments():
     from jerald_gb300 import _lib
     from jerald_gb300.ldl import FusedLDL
