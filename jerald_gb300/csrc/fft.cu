@@ -177,6 +177,13 @@ static int plan_for_call(cudaStream_t st, int nx, int ny, int nz, Plan3<T>* pl) 
 // ---------------------------------------------------------------------------
 // Full transforms.
 
+// Complex buffers (and the real input of r2c / output of c2r, which the
+// passes access as pairs) must be aligned to one complex element.
+template <typename T>
+static bool cplx_aligned(const void* p) {
+  return ((uintptr_t)p % sizeof(cplx_t<T>)) == 0;
+}
+
 template <typename T>
 static int fft_args_check(int nx, int ny, int nz, const void* ws, size_t ws_bytes,
                           const char* who) {
@@ -334,6 +341,9 @@ static int rfft3(cudaStream_t st, const T* data, int nx, int ny, int nz, cplx_t<
   if (s) return s;
   if (!data || (!out_c && (!out_re || !out_im)))
     return set_error(JLD_ERR_ARG, "%s: NULL data or output", who);
+  if (!cplx_aligned<T>(data) || !cplx_aligned<T>(ws) || (out_c && !cplx_aligned<T>(out_c)))
+    return set_error(JLD_ERR_ARG, "%s: data, workspace and complex output must be %zu-byte aligned", who,
+                     sizeof(cplx_t<T>));
   Plan3<T> pl;
   if ((s = plan_for_call<T>(st, nx, ny, nz, &pl))) return s;
   const int h = pl.h;
@@ -362,6 +372,9 @@ static int irfft3(cudaStream_t st, const cplx_t<T>* in_c, const T* in_re, const 
   if (s) return s;
   if (!out || (!in_c && (!in_re || !in_im)))
     return set_error(JLD_ERR_ARG, "%s: NULL input or output", who);
+  if (!cplx_aligned<T>(out) || !cplx_aligned<T>(ws) || (in_c && !cplx_aligned<T>(in_c)))
+    return set_error(JLD_ERR_ARG, "%s: output, workspace and complex input must be %zu-byte aligned", who,
+                     sizeof(cplx_t<T>));
   Plan3<T> pl;
   if ((s = plan_for_call<T>(st, nx, ny, nz, &pl))) return s;
   const int h = pl.h;
@@ -443,6 +456,8 @@ __global__ void static_twiddles_kernel(float2* tw, int n, int count) {
 static int pfft_static_impl(cudaStream_t st, const float* data, int nx, int ny, int nz, float2* out_c) {
   const char* who = "jld_pfft_c_static_f32";
   if (!data || !out_c) return set_error(JLD_ERR_ARG, "%s: NULL data or output", who);
+  if (!cplx_aligned<float>(data) || !cplx_aligned<float>(out_c))
+    return set_error(JLD_ERR_ARG, "%s: data and output must be 8-byte aligned", who);
   if (nx < 1 || ny < 1 || nz < 2) return set_error(JLD_ERR_ARG, "%s: mesh sizes must be positive (nz >= 2)", who);
   if (nz & 1) return set_error(JLD_ERR_UNSUPPORTED, "%s: nz must be even", who);
   if (nx > kStaticMaxLen || ny > kStaticMaxLen || nz > kStaticMaxLen)

@@ -295,27 +295,34 @@ def test_pifft_matches_definition(jl, dt, nm):
 
 
 @pytest.mark.parametrize("nm", [(64, 64, 64), (256, 64, 512)])
-def test_fft_unaligned_pointers_take_generic_passes(jl, nm):
-    # a 4-byte offset input / output cannot feed bulk or tensor copies: the
-    # call must fall back to the generic passes and give the same transform
+def test_fft_alignment_fallback_and_rejection(jl, nm):
+    # 8-byte aligned (not 16) input / output: no bulk or tensor copies, the
+    # generic passes run and give the same transform.  4-byte aligned: the
+    # complex-pair accesses cannot run at all, so the call is rejected on
+    # the host before any launch.
+    from jerald_gb300 import _lib
     x = torch.randn(nm, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
-    xo = torch.empty(x.numel() + 1, device="cuda")
-    xo[1:] = x.reshape(-1)
-    xu = xo[1:]
+    xo = torch.empty(x.numel() + 2, device="cuda")
+    xo[2:] = x.reshape(-1)
     h = nm[2] // 2 + 1
     ws = _ws(jl, nm, np.float32)
     a = torch.empty(nm[:2] + (h,), dtype=torch.complex64, device="cuda")
     b = torch.empty_like(a)
     jl.call("jld_pfft_c_f32", _st(), _p(x), *nm, _p(a), _p(ws), ws.numel())
-    jl.call("jld_pfft_c_f32", _st(), _p(xu), *nm, _p(b), _p(ws), ws.numel())
+    jl.call("jld_pfft_c_f32", _st(), ct.c_void_p(xo.data_ptr() + 8), *nm, _p(b), _p(ws), ws.numel())
     scale = a.abs().pow(2).mean().sqrt().item()
     assert (a - b).abs().max().item() / scale < 2e-6 * np.log2(x.numel())
-    yo = torch.empty(x.numel() + 1, device="cuda")
+    yo = torch.empty(x.numel() + 2, device="cuda")
     ya = torch.empty(nm, device="cuda")
     jl.call("jld_pifft_c_f32", _st(), _p(a), *nm, _p(ya), _p(ws), ws.numel())
-    jl.call("jld_pifft_c_f32", _st(), _p(a), *nm, ct.c_void_p(yo.data_ptr() + 4), _p(ws), ws.numel())
-    yb = yo[1:].reshape(nm)
+    jl.call("jld_pifft_c_f32", _st(), _p(a), *nm, ct.c_void_p(yo.data_ptr() + 8), _p(ws), ws.numel())
+    yb = yo[2:].reshape(nm)
     assert (ya - yb).abs().max().item() / ya.abs().max().item() < 1e-5
+    with pytest.raises(_lib.JLDError) as e:
+        jl.call("jld_pfft_c_f32", _st(), ct.c_void_p(xo.data_ptr() + 4), *nm, _p(b), _p(ws), ws.numel())
+    assert e.value.status == 1
+    with pytest.raises(_lib.JLDError):
+        jl.call("jld_pifft_c_f32", _st(), _p(a), *nm, ct.c_void_p(yo.data_ptr() + 4), _p(ws), ws.numel())
     v = ct.c_int32(-1)
     jl.call("jld_fft_pipe_status", ct.byref(v), 1)
     assert v.value == 0
