@@ -239,7 +239,7 @@ static int ldl_step(const StepArgs& a) {
     zr2c = zpipe_geom(rows, h, 1, (size_t)h * 8);
     zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8);
     zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8);
-    zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16, 120 * 1024);
+    zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16);
   }
   // the generic kernels then only cover the nyq plane
   SpecPass gxn = gx.sp, gyn = gy.sp;
@@ -379,25 +379,41 @@ static int ldl_step(const StepArgs& a) {
     return JLD_OK;
   };
 
-  // ---------------- forward layers
+  // With plain atomics the update of layer l paints X_{l+1} in the same
+  // kernel, and the adjoint of layer l folds in the paint adjoint of layer
+  // l+1 (no separate gather kernels, no cotangent round trip).
+  const bool fuse_paint = !a.binned && a.paint_method == 0;
+  const bool fuse_adj = !a.binned;
+
+  // ---------------- forward layers (density of layer l+1 painted at its update)
+  if ((s = paint_into(Xl(0), rho))) return s;
   for (int l = 0; l < a.nstep; ++l) {
     float4* g4_l = g4_of(l);
-    if ((s = paint_into(Xl(l), rho + (size_t)L.C * l))) return s;
     if ((s = force_mesh(l, g4_l))) return s;
-    update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
-    JLD_LAUNCH_CHECK("update_kernel");
+    float* rho_next = rho + (size_t)L.C * (l + 1);  // the final map for l = nstep-1
+    float* X_next = Xs + (size_t)3 * a.N * l;
+    if (fuse_paint) {
+      JLD_CUDA_TRY(cudaMemsetAsync(rho_next, 0, sizeof(float) * L.C, st));
+      update_paint_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, X_next, rho_next);
+      JLD_LAUNCH_CHECK("update_paint_kernel");
+    } else {
+      update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, X_next);
+      JLD_LAUNCH_CHECK("update_kernel");
+      if ((s = paint_into(Xl(l + 1), rho_next))) return s;
+    }
   }
 
   // ---------------- final map, loss and its cotangent
   float* rho_f = rho + (size_t)L.C * a.nstep;
-  if ((s = paint_into(Xl(a.nstep), rho_f))) return s;
   loss_kernel<<<cgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
                                         a.L1, npix, rb, part);
   JLD_LAUNCH_CHECK("loss_kernel");
   launch_finish(st, part, (int)cgrid, 4, 1, a.out, 0, npix);
   if (a.kind == 0) launch_finish(st, part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
-  gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
-  JLD_LAUNCH_CHECK("gather_vjp_kernel");
+  if (!fuse_adj) {
+    gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
+    JLD_LAUNCH_CHECK("gather_vjp_kernel");
+  }
 
   // ---------------- adjoint layers
   for (int l = a.nstep - 1; l >= 0; --l) {
@@ -419,12 +435,15 @@ static int ldl_step(const StepArgs& a) {
                                                           Xb2);
       JLD_LAUNCH_CHECK("tiled_bwd_kernel");
     } else {
+      // cotangent of X_{l+1}: the previous layer's output plus the paint
+      // adjoint of rho_{l+1} (rb holds it: the loss's for the last layer);
       // the first layer's input positions are data: scatter only
+      const float* Xbp = (l == a.nstep - 1) ? nullptr : Xb;
       if (l > 0)
-        bwd_particles_kernel<true><<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
+        bwd_fused_kernel<true><<<pgrid, pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
       else
-        bwd_particles_kernel<false><<<pgrid, pblock, 0, st>>>(Xl(l), Xb, a.N, bg, g, g4_l, gb4, Xb2);
-      JLD_LAUNCH_CHECK("bwd_particles_kernel");
+        bwd_fused_kernel<false><<<pgrid, pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
+      JLD_LAUNCH_CHECK("bwd_fused_kernel");
     }
     if (zr2c3.ok) {
       s = with_p2(h, [&](auto sch) {
@@ -532,7 +551,7 @@ static int ldl_step(const StepArgs& a) {
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv_adj_kernel");
     launch_finish(st, part, (int)adj_blocks, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
-    if (l > 0) {
+    if (l > 0 && !fuse_adj) {
       gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
       JLD_LAUNCH_CHECK("gather_vjp_kernel");
     }

@@ -9,13 +9,18 @@
 //   yinv3      Gy = iFFT_y(-i c_y T0), Gz = -i c_z iFFT_y(T0), Gx = iFFT_y(T1)
 //   zinv3      three c2r rows -> float4 force mesh (gx, gy, gz, 0)  zinv3_kernel
 //   update     X' = X + CIC gather of the force mesh                update_kernel
+//              (update_paint_kernel also paints X': the next density)
 // Final map and loss (model.py:311-403): paint, loss_kernel (bias, ReLU,
-// L1/L2 with mask, its cotangent and d/d(mu, w, b)), gather_vjp_kernel.
+// L1/L2 with mask, its cotangent and d/d(mu, w, b)), gather_vjp_kernel
+// (folded into bwd_fused_kernel on the plain-atomic path).
+// The pipelined (TMA / bulk-copy) versions of the FFT passes are in
+// ldl_pipe.cuh and zpipe.cuh.
 // Adjoint of one layer, given Xbar' (the cotangent of X'):
-//   bwd_particles  Xbar = Xbar' + sum_d Xbar'_d grad g_d(X)  (gather of the
-//                  float4 force mesh with CIC weight gradients) and the
-//                  3-channel scatter gbar_d = paint(X, Xbar'_d) as one float4
-//                  vector atomic per corner
+//   bwd_fused  Xbar' completed with the paint adjoint of the next layer's
+//              density, then Xbar = Xbar' + sum_d Xbar'_d grad g_d(X) (gather
+//              of the float4 force mesh with CIC weight gradients) and the
+//              3-channel scatter gbar_d = paint(X, Xbar'_d) as one float4
+//              vector atomic per corner
 //   zfwd3      r2c of gbar_x, gbar_y, gbar_z; the z channel is multiplied by c_z
 //   yfwd_comb  Bx = FFT_y(Ax), D = c_y FFT_y(Ay) + FFT_y(c_z Az)
 //   xbwd       W = i (c_x FFT_x(Bx) + FFT_x(D)); reductions for d/d(alpha,
@@ -418,38 +423,158 @@ update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
   }
 }
 
-// Adjoint of one layer's readout, per particle: Xbar = Xbar' + J^T Xbar'
-// (gather of the float4 force mesh with weight gradients) and the scatter of
-// Xbar' into the float4 cotangent mesh.  GATHER = false (the first layer,
-// whose input positions need no cotangent) does the scatter only.
-template <bool GATHER>
-__global__ void __launch_bounds__(256, 4)
-bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1, int64_t n,
-                     BoxGeom bg, Grid3 g, const float4* __restrict__ g4, float4* __restrict__ gb4,
-                     float* __restrict__ Xb) {
+// Xbar += sum_c rb[c] grad w_c (the adjoint of a unit-mass paint,
+// lib/parops_fast.h:730-821 with vjp = true); accumulate == 0 overwrites.
+__global__ void __launch_bounds__(256)
+gather_vjp_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
+                  const float* __restrict__ rb, float* __restrict__ Xb, int accumulate) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    Corners<float> c;
+    float lo[3], hi[3];
+    particle_setup(X, p, bg, g, c, lo, hi);
+    float a[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      int bits = corner_axis_bits(k);
+      if (!corner_ok(c, bits)) continue;
+      float r = __ldg(rb + corner_offset(c, bits, g));
+#pragma unroll
+      for (int e = 0; e < 3; ++e) {
+        float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
+        l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
+        a[e] += r * wprod(l2, h2, bits);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 3; ++e) Xb[3 * p + e] = accumulate ? Xb[3 * p + e] + a[e] : a[e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused particle kernels (plain-atomic scatter path).
+
+// Unit-weight scatter of one particle's eight corner weights with the 16 x 2
+// pairing (warp-collective: every lane of the warp calls it; dead lanes pass
+// live = false and zero weights).
+__device__ __forceinline__ void paired_scatter(float* __restrict__ out, const Corners<float>& c, const Grid3& g,
+                                               float (&w)[8], bool live) {
   const unsigned full = 0xffffffffu;
-  // warp tasks of the 16 x 2 pairing layout (row-length hint nz); a dead
-  // lane re-reads the last particle with a zero cotangent and stores nothing
+  const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
+    if (pr.tz) w[zpair_lo(j)] = __fadd_rn(w[zpair_lo(j)], t);
+  }
+  const float t2 = __shfl_up_sync(full, w[2], 16), t4 = __shfl_up_sync(full, w[4], 16);
+  const float t6 = __shfl_up_sync(full, w[6], 16), t7 = __shfl_up_sync(full, w[7], 16);
+  if (pr.ty) { w[0] = __fadd_rn(w[0], t2); w[1] = __fadd_rn(w[1], t4); }
+  if (pr.thz) { w[3] = __fadd_rn(w[3], t6); w[5] = __fadd_rn(w[5], t7); }
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (pair_keeps(pr, k)) atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
+  }
+}
+
+// X' = X + readout of the float4 force mesh (update_kernel's arithmetic),
+// stored, then X' painted with unit mass into rho (zeroed by the caller):
+// the next layer's density (or the final map) without re-reading X'.
+__global__ void __launch_bounds__(256, 5)
+update_paint_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
+                    const float4* __restrict__ g4, float* __restrict__ Xn, float* __restrict__ rho) {
   for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
     const int64_t pp = pw.particle();
     const bool live = pp >= 0;
     const int64_t p = live ? pp : n - 1;
+    float xn[3];
+    {
+      Corners<float> c;
+      float lo[3], hi[3];
+      particle_setup(X, p, bg, g, c, lo, hi);
+      float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int bits = corner_axis_bits(k);
+        const float4 v = __ldg(g4 + corner_offset(c, bits, g));
+        const float w = corner_ok(c, bits) ? wprod(lo, hi, bits) : 0.f;
+        const float t0 = __fmul_rn(w, v.x), t1 = __fmul_rn(w, v.y), t2 = __fmul_rn(w, v.z);
+        if (k == 0) { acc[0] = t0; acc[1] = t1; acc[2] = t2; }
+        else { acc[0] = __fadd_rn(acc[0], t0); acc[1] = __fadd_rn(acc[1], t1); acc[2] = __fadd_rn(acc[2], t2); }
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) xn[a] = __fadd_rn(__ldg(X + 3 * p + a), acc[a]);
+    }
+    if (live) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) Xn[3 * p + a] = xn[a];
+    }
+    float q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) q[a] = box_to_mesh(xn[a], bg.box[a], bg.cell[a]);
+    Corners<float> c;
+    cic_corners(q, g, c);
+    float lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = __fsub_rn(1.f, c.d[a]); }
+    float w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int bits = corner_axis_bits(k);
+      w[k] = (live && corner_ok(c, bits)) ? wprod(lo, hi, bits) : 0.f;
+    }
+    paired_scatter(rho, c, g, w, live);
+  }
+}
+
+// Adjoint of layer l with the paint adjoint of layer l+1 folded in:
+//   v = Xbp + sum_c rb[c] grad w_c(Xn)     (gather_vjp_kernel's arithmetic;
+//                                           Xbp == nullptr: no partial)
+//   Xb = v + J^T v at X (GATHER), gb4 += scatter of v (bwd_particles_kernel)
+// Xn are the positions after layer l, X the positions before it.
+template <bool GATHER>
+__global__ void __launch_bounds__(256, 4)
+bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, const float* __restrict__ Xbp,
+                 const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g, const float4* __restrict__ g4,
+                 float4* __restrict__ gb4, float* __restrict__ Xb) {
+  const unsigned full = 0xffffffffu;
+  for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
+    const int64_t pp = pw.particle();
+    const bool live = pp >= 0;
+    const int64_t p = live ? pp : n - 1;
+    float v[3];
+    {
+      Corners<float> c;
+      float lo[3], hi[3];
+      particle_setup(Xn, p, bg, g, c, lo, hi);
+      float a[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int bits = corner_axis_bits(k);
+        if (!corner_ok(c, bits)) continue;
+        const float r = __ldg(rb + corner_offset(c, bits, g));
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
+          l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
+          a[e] += r * wprod(l2, h2, bits);
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 3; ++e) v[e] = live ? (Xbp ? __ldg(Xbp + 3 * p + e) + a[e] : a[e]) : 0.f;
+    }
     Corners<float> c;
     float lo[3], hi[3];
     particle_setup(X, p, bg, g, c, lo, hi);
-    float v[3] = {0.f, 0.f, 0.f};
-    if (live) {
-      v[0] = __ldg(Xb1 + 3 * p); v[1] = __ldg(Xb1 + 3 * p + 1); v[2] = __ldg(Xb1 + 3 * p + 2);
-    }
     float a[3] = {0.f, 0.f, 0.f};
     float4 s4[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      int bits = corner_axis_bits(k);
-      bool ok = corner_ok(c, bits);
+      const int bits = corner_axis_bits(k);
+      const bool ok = corner_ok(c, bits);
       if (GATHER) {
-        float4 gv = __ldg(g4 + corner_offset(c, bits, g));
-        float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
+        const float4 gv = __ldg(g4 + corner_offset(c, bits, g));
+        const float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
           float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
@@ -457,7 +582,7 @@ bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1,
           a[e] += ok ? u * wprod(l2, h2, bits) : 0.f;
         }
       }
-      float w = ok ? wprod(lo, hi, bits) : 0.f;
+      const float w = ok ? wprod(lo, hi, bits) : 0.f;
       s4[k] = make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f);
     }
     const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
@@ -485,34 +610,6 @@ bwd_particles_kernel(const float* __restrict__ X, const float* __restrict__ Xb1,
         for (int e = 0; e < 3; ++e) Xb[3 * p + e] = v[e] + a[e];
       }
     }
-  }
-}
-
-// Xbar += sum_c rb[c] grad w_c (the adjoint of a unit-mass paint,
-// lib/parops_fast.h:730-821 with vjp = true); accumulate == 0 overwrites.
-__global__ void __launch_bounds__(256)
-gather_vjp_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
-                  const float* __restrict__ rb, float* __restrict__ Xb, int accumulate) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    Corners<float> c;
-    float lo[3], hi[3];
-    particle_setup(X, p, bg, g, c, lo, hi);
-    float a[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      int bits = corner_axis_bits(k);
-      if (!corner_ok(c, bits)) continue;
-      float r = __ldg(rb + corner_offset(c, bits, g));
-#pragma unroll
-      for (int e = 0; e < 3; ++e) {
-        float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
-        l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
-        a[e] += r * wprod(l2, h2, bits);
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < 3; ++e) Xb[3 * p + e] = accumulate ? Xb[3 * p + e] + a[e] : a[e];
   }
 }
 
