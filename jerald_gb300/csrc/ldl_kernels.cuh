@@ -9,7 +9,6 @@
 //   yinv3      Gy = iFFT_y(-i c_y T0), Gz = -i c_z iFFT_y(T0), Gx = iFFT_y(T1)
 //   zinv3      three c2r rows -> float4 force mesh (gx, gy, gz, 0)  zinv3_kernel
 //   update     X' = X + CIC gather of the force mesh                update_kernel
-//              (update_paint_kernel also paints X': the next density)
 // Final map and loss (model.py:311-403): paint, loss_kernel (bias, ReLU,
 // L1/L2 with mask, its cotangent and d/d(mu, w, b)), gather_vjp_kernel
 // (folded into bwd_fused_kernel on the plain-atomic path).
@@ -453,79 +452,6 @@ gather_vjp_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
 
 // ---------------------------------------------------------------------------
 // Fused particle kernels (plain-atomic scatter path).
-
-// Unit-weight scatter of one particle's eight corner weights with the 16 x 2
-// pairing (warp-collective: every lane of the warp calls it; dead lanes pass
-// live = false and zero weights).
-__device__ __forceinline__ void paired_scatter(float* __restrict__ out, const Corners<float>& c, const Grid3& g,
-                                               float (&w)[8], bool live) {
-  const unsigned full = 0xffffffffu;
-  const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const float t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
-    if (pr.tz) w[zpair_lo(j)] = __fadd_rn(w[zpair_lo(j)], t);
-  }
-  const float t2 = __shfl_up_sync(full, w[2], 16), t4 = __shfl_up_sync(full, w[4], 16);
-  const float t6 = __shfl_up_sync(full, w[6], 16), t7 = __shfl_up_sync(full, w[7], 16);
-  if (pr.ty) { w[0] = __fadd_rn(w[0], t2); w[1] = __fadd_rn(w[1], t4); }
-  if (pr.thz) { w[3] = __fadd_rn(w[3], t6); w[5] = __fadd_rn(w[5], t7); }
-  if (live) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (pair_keeps(pr, k)) atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
-  }
-}
-
-// X' = X + readout of the float4 force mesh (update_kernel's arithmetic),
-// stored, then X' painted with unit mass into rho (zeroed by the caller):
-// the next layer's density (or the final map) without re-reading X'.
-__global__ void __launch_bounds__(256, 5)
-update_paint_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
-                    const float4* __restrict__ g4, float* __restrict__ Xn, float* __restrict__ rho) {
-  for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
-    const int64_t pp = pw.particle();
-    const bool live = pp >= 0;
-    const int64_t p = live ? pp : n - 1;
-    float xn[3];
-    {
-      Corners<float> c;
-      float lo[3], hi[3];
-      particle_setup(X, p, bg, g, c, lo, hi);
-      float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int bits = corner_axis_bits(k);
-        const float4 v = __ldg(g4 + corner_offset(c, bits, g));
-        const float w = corner_ok(c, bits) ? wprod(lo, hi, bits) : 0.f;
-        const float t0 = __fmul_rn(w, v.x), t1 = __fmul_rn(w, v.y), t2 = __fmul_rn(w, v.z);
-        if (k == 0) { acc[0] = t0; acc[1] = t1; acc[2] = t2; }
-        else { acc[0] = __fadd_rn(acc[0], t0); acc[1] = __fadd_rn(acc[1], t1); acc[2] = __fadd_rn(acc[2], t2); }
-      }
-#pragma unroll
-      for (int a = 0; a < 3; ++a) xn[a] = __fadd_rn(__ldg(X + 3 * p + a), acc[a]);
-    }
-    if (live) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) Xn[3 * p + a] = xn[a];
-    }
-    float q[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) q[a] = box_to_mesh(xn[a], bg.box[a], bg.cell[a]);
-    Corners<float> c;
-    cic_corners(q, g, c);
-    float lo[3], hi[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = __fsub_rn(1.f, c.d[a]); }
-    float w[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int bits = corner_axis_bits(k);
-      w[k] = (live && corner_ok(c, bits)) ? wprod(lo, hi, bits) : 0.f;
-    }
-    paired_scatter(rho, c, g, w, live);
-  }
-}
 
 // Adjoint of layer l with the paint adjoint of layer l+1 folded in:
 //   v = Xbp + sum_c rb[c] grad w_c(Xn)     (gather_vjp_kernel's arithmetic;
