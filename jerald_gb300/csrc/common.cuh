@@ -91,6 +91,25 @@ __device__ __forceinline__ T box_to_mesh(T x, T box, T cell) {
   return r / cell;
 }
 
+// The same prelude with r * (N/L) instead of r / (L/N): one rounding more
+// (q within an ulp or two of box_to_mesh's), no division.  For kernels whose
+// results are compared within a tolerance (the fused step): the CIC weights
+// are continuous in q, so painted and gathered values move by a few ulps.
+__device__ __forceinline__ float box_to_mesh_fast(float x, float box, float inv_cell) {
+  float r;
+  if (x >= 0.f && x < box) {
+    r = x;
+  } else if (x >= box && x < 2.f * box) {
+    r = x - box;
+  } else if (x < 0.f && x > -box) {
+    r = x + box;
+  } else {
+    r = fmodf(x, box);
+    if (r != 0.f && ((r < 0.f) != (box < 0.f))) r = r + box;
+  }
+  return r * inv_cell;
+}
+
 // IEEE round-to-nearest products/sums without FMA contraction, so that the
 // CIC weights and readout sums follow the reference's operation order
 // (lib/parops_fast.h:376-409, 442-478) bit for bit.

@@ -384,10 +384,37 @@ __device__ __forceinline__ void particle_setup(const float* __restrict__ X, int6
                                                float lo[3], float hi[3]) {
   float q[3];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) q[a] = box_to_mesh(__ldg(X + 3 * p + a), bg.box[a], bg.cell[a]);
+  for (int a = 0; a < 3; ++a) q[a] = box_to_mesh_fast(__ldg(X + 3 * p + a), bg.box[a], bg.dw[a]);
   cic_corners(q, g, c);
 #pragma unroll
   for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = __fsub_rn(1.f, c.d[a]); }
+}
+
+// sum_k u_k grad w_k over the eight corners (u_k = 0 for invalid corners),
+// factored by axis: d w_k / d x_0 = (b_x ? dw_0 : -dw_0) w_y[b_y] w_z[b_z]
+// and likewise for y and z, so each axis costs four differences and four
+// products of the other two axes' weights.
+__device__ __forceinline__ void cic_grad(const float (&u)[8], const float lo[3], const float hi[3],
+                                         const float dw[3], float out[3]) {
+  float U[2][2][2];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int b = corner_axis_bits(k);
+    U[b & 1][(b >> 1) & 1][(b >> 2) & 1] = u[k];
+  }
+  const float wx[2] = {lo[0], hi[0]}, wy[2] = {lo[1], hi[1]}, wz[2] = {lo[2], hi[2]};
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      sx += wy[i] * wz[j] * (U[1][i][j] - U[0][i][j]);
+      sy += wx[i] * wz[j] * (U[i][1][j] - U[i][0][j]);
+      sz += wx[i] * wy[j] * (U[i][j][1] - U[i][j][0]);
+    }
+  out[0] = dw[0] * sx;
+  out[1] = dw[1] * sy;
+  out[2] = dw[2] * sz;
 }
 
 __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int bits) {
@@ -473,19 +500,14 @@ bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, con
       Corners<float> c;
       float lo[3], hi[3];
       particle_setup(Xn, p, bg, g, c, lo, hi);
-      float a[3] = {0.f, 0.f, 0.f};
+      float r[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         const int bits = corner_axis_bits(k);
-        if (!corner_ok(c, bits)) continue;
-        const float r = __ldg(rb + corner_offset(c, bits, g));
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
-          l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
-          a[e] += r * wprod(l2, h2, bits);
-        }
+        r[k] = corner_ok(c, bits) ? __ldg(rb + corner_offset(c, bits, g)) : 0.f;
       }
+      float a[3];
+      cic_grad(r, lo, hi, bg.dw, a);
 #pragma unroll
       for (int e = 0; e < 3; ++e) v[e] = live ? (Xbp ? __ldg(Xbp + 3 * p + e) + a[e] : a[e]) : 0.f;
     }
@@ -494,21 +516,20 @@ bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, con
     particle_setup(X, p, bg, g, c, lo, hi);
     float a[3] = {0.f, 0.f, 0.f};
     float4 s4[8];
+    if (GATHER) {
+      float u[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int bits = corner_axis_bits(k);
+        const float4 gv = __ldg(g4 + corner_offset(c, bits, g));
+        u[k] = corner_ok(c, bits) ? v[0] * gv.x + v[1] * gv.y + v[2] * gv.z : 0.f;
+      }
+      cic_grad(u, lo, hi, bg.dw, a);
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int bits = corner_axis_bits(k);
-      const bool ok = corner_ok(c, bits);
-      if (GATHER) {
-        const float4 gv = __ldg(g4 + corner_offset(c, bits, g));
-        const float u = v[0] * gv.x + v[1] * gv.y + v[2] * gv.z;
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          float l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]};
-          l2[e] = -bg.dw[e]; h2[e] = bg.dw[e];
-          a[e] += ok ? u * wprod(l2, h2, bits) : 0.f;
-        }
-      }
-      const float w = ok ? wprod(lo, hi, bits) : 0.f;
+      const float w = corner_ok(c, bits) ? wprod(lo, hi, bits) : 0.f;
       s4[k] = make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f);
     }
     const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
