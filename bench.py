@@ -185,11 +185,12 @@ def time_primitives(pos, n, box, steps, warmup):
 
 def count_launches(nstep: int, kind: str, mask: bool, recompute: bool = False) -> int:
     """Kernel launches of one fused step on a power-of-two mesh with the
-    pipelined passes (used only when the captured graph cannot be asked)."""
-    force_mesh = 8                      # z r2c, y pass (2), x filter (2), inverse y (2), inverse z
-    fwd = nstep * (1 + force_mesh + 1)  # paint, force mesh, update
-    final = 1 + 1 + (2 if kind == "sm" else 1) + 1 + (1 if mask else 0)
-    adj = nstep * 12 + (nstep - 1)      # + position cotangent gathers of layers >= 1
+    pipelined passes and plain atomics (used only when the captured graph
+    cannot be asked)."""
+    force_mesh = 8                              # z r2c, y pass (2), x filter (2), inverse y (2), inverse z
+    fwd = 1 + nstep * (force_mesh + 2)          # first paint; per layer force mesh, update, paint
+    final = 1 + (2 if kind == "sm" else 1) + (1 if mask else 0)   # loss, its reductions (+ mask count)
+    adj = nstep * 12                            # fused particle adjoint + 11 spectral / reduction kernels
     rec = force_mesh * max(0, nstep - 2) if recompute else 0
     return 1 + fwd + final + adj + rec
 
@@ -433,29 +434,25 @@ def main():
     loss, grad = step.out[0].item(), step.out[1:].cpu().numpy()
     assert step.error_word() == 0, "a pipelined pass gave up waiting for a copy"
 
-    # e2e: host buffers -> device, step, loss+grads -> host
+    # e2e: host buffers -> device, step, loss+grads -> host, through the
+    # public host feed (copies of step k+1 overlap the compute of step k)
+    from jerald_gb300.ldl import HostFeed
     pos_h = pos.cpu().pin_memory()
     tgt_h = target.cpu().pin_memory()
-    out_h = torch.empty(step.out.shape, dtype=torch.float64).pin_memory()
     h2d = pos_h.numel() * 4 + tgt_h.numel() * 4
-    d2h = out_h.numel() * 8
-    for _ in range(args.warmup):
-        pos.copy_(pos_h, non_blocking=True)
-        target.copy_(tgt_h, non_blocking=True)
-        step.replay(params)
-        out_h.copy_(step.out, non_blocking=True)
+    feed = HostFeed(step)
+    out_h = torch.empty((max(args.steps, args.warmup), step.out.numel()), dtype=torch.float64).pin_memory()
+    d2h = step.out.numel() * 8
+    feed.run([(pos_h, tgt_h)] * args.warmup, params, out_h)
     barrier()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2.record(st)
-    for _ in range(args.steps):
-        pos.copy_(pos_h, non_blocking=True)
-        target.copy_(tgt_h, non_blocking=True)
-        step.replay(params)
-        out_h.copy_(step.out, non_blocking=True)
+    feed.run([(pos_h, tgt_h)] * args.steps, params, out_h)
     e3.record(st)
     barrier()
+    e2e_loss_err = abs(float(out_h[args.steps - 1, 0]) - loss) / abs(loss)
     e2e_value, ms_e2e = replicas.aggregate_rate(e2.elapsed_time(e3) / args.steps, dev)
-    del pos_h, tgt_h
+    del pos_h, tgt_h, feed
 
     extra = {}
     peak, peak_kind = _peaks()
@@ -516,7 +513,9 @@ def main():
                            else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+                        "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
+                        "path": "FusedLDL + HostFeed (double-buffered pinned-host copies)",
+                        "loss_rel_diff_vs_device_run": e2e_loss_err},
                 "gpu_launches": (launches_per_step if launches_per_step is not None
                                  else count_launches(nstep, "sm", False, args.recompute)) * args.steps,
                 "clocks": clk.summary(), "loss": loss, **extra}

@@ -24,6 +24,8 @@ struct PosSrc {
   const T* pos;   // (N, 3) row-major
   T box[3];       // used when BOX
   T cell[3];      // box / N per axis, in T
+  T inv[3];       // N / box per axis (fast prelude)
+  int fast;       // 1: box_to_mesh_fast (the fused step's paints, float only)
 };
 
 template <typename T, bool BOX>
@@ -31,6 +33,14 @@ __device__ __forceinline__ void load_pos(const PosSrc<T>& s, int64_t p, T q[3]) 
   const T* src = s.pos + 3 * p;
   T x = __ldg(src), y = __ldg(src + 1), z = __ldg(src + 2);
   if (BOX) {
+    if constexpr (sizeof(T) == 4) {
+      if (s.fast) {
+        q[0] = box_to_mesh_fast(x, s.box[0], s.inv[0]);
+        q[1] = box_to_mesh_fast(y, s.box[1], s.inv[1]);
+        q[2] = box_to_mesh_fast(z, s.box[2], s.inv[2]);
+        return;
+      }
+    }
     q[0] = box_to_mesh(x, s.box[0], s.cell[0]);
     q[1] = box_to_mesh(y, s.box[1], s.cell[1]);
     q[2] = box_to_mesh(z, s.box[2], s.cell[2]);
@@ -284,14 +294,16 @@ static PosSrc<T> make_src(const T* pos, const T* box, int64_t nx, int64_t ny,
   for (int a = 0; a < 3; ++a) {
     s.box[a] = box ? box[a] : T(1);
     s.cell[a] = box ? (T)(box[a] / (T)n[a]) : T(1);
+    s.inv[a] = box ? (T)((T)n[a] / box[a]) : T(1);
   }
+  s.fast = 0;
   return s;
 }
 
 template <typename T>
 static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* mass,
                       T mscalar, int64_t nx, int64_t ny, int64_t nz, const T* box,
-                      int method, T* out, const char* who) {
+                      int method, T* out, const char* who, bool fast = false) {
   int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
   if (s) return s;
   if (box && !(box[0] > 0 && box[1] > 0 && box[2] > 0))
@@ -300,6 +312,7 @@ static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* ma
   JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(T) * g.cells(), st));
   if (nparts == 0) return JLD_OK;
   PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
+  src.fast = fast ? 1 : 0;
   const int block = 256;
   unsigned grid = grid_for(nparts, block);
   if (method == 1) {
@@ -380,7 +393,7 @@ static int readout3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T*
 
 int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny,
                    int64_t nz, const float* box, int method, float* out) {
-  return paint_impl<float>(st, pos, n, nullptr, 1.0f, nx, ny, nz, box, method, out, "fused paint");
+  return paint_impl<float>(st, pos, n, nullptr, 1.0f, nx, ny, nz, box, method, out, "fused paint", true);
 }
 
 template <typename T>

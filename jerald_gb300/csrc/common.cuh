@@ -47,7 +47,8 @@ inline unsigned grid_for(int64_t n, int block, int per_sm = 8) {
 }
 
 // Unit-mass CIC paint of box-unit positions into `out` (zeroed first); the
-// same kernels as jld_ppaint_box_f32 (method 0 atomics, 1 warp-aggregated).
+// same kernels as jld_ppaint_box_f32 (method 0 atomics, 1 warp-aggregated)
+// with the division-free prelude (box_to_mesh_fast).
 int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny,
                    int64_t nz, const float* box, int method, float* out);
 

@@ -113,18 +113,24 @@ class FusedLDL:
         self._launch(pos, target, mask)
         return self.out[0], self.out[1:]
 
-    def capture(self, pos, target, mask=None):
-        """Captures the step on static inputs (they must stay alive and in place)."""
-        self._static = (pos, target, mask)
+    def capture_graph(self, pos, target, mask=None):
+        """A new CUDA graph of the step on these (static) inputs; the step's
+        own graph is left as it is."""
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
             self._launch(pos, target, mask)  # builds plans, tables and kernel attributes
         torch.cuda.current_stream(self.device).wait_stream(s)
-        self.graph = _new_graph()
-        with torch.cuda.graph(self.graph):
+        g = _new_graph()
+        with torch.cuda.graph(g):
             self._launch(pos, target, mask)
-        _finish_capture(self.graph)
+        _finish_capture(g)
+        return g
+
+    def capture(self, pos, target, mask=None):
+        """Captures the step on static inputs (they must stay alive and in place)."""
+        self._static = (pos, target, mask)
+        self.graph = self.capture_graph(pos, target, mask)
         return self.graph
 
     def replay(self, params=None):
@@ -172,3 +178,57 @@ class FusedLDL:
         out = torch.empty_like(x)
         out[perm] = x
         return out
+
+
+class HostFeed:
+    """Runs a FusedLDL from host-resident inputs, one step per input pair,
+    with the host-to-device copies of step k+1 overlapped with the compute
+    of step k: two device input buffers with one captured graph each, a copy
+    stream and events.  Every step's positions and target are copied from
+    (pinned) host memory and its loss and gradient are read back; only the
+    order of the copies changes, not their amount.
+    """
+
+    def __init__(self, step: FusedLDL, mask=None):
+        self.step = step
+        dev = step.device
+        self.pos = [torch.empty((step.nparts, 3), dtype=torch.float32, device=dev) for _ in range(2)]
+        self.tgt = [torch.empty(step.nmesh, dtype=torch.float32, device=dev) for _ in range(2)]
+        for t in self.pos + self.tgt:
+            t.zero_()
+        self.mask = mask
+        self.graphs = [step.capture_graph(self.pos[b], self.tgt[b], mask) for b in range(2)]
+        self.copy = torch.cuda.Stream(dev)
+        self.copied = [torch.cuda.Event() for _ in range(2)]
+        self.free = [torch.cuda.Event() for _ in range(2)]
+
+    def run(self, inputs, params, out_host: torch.Tensor) -> None:
+        """inputs: sequence of (pos, target) host tensors (pinned for
+        asynchronous copies); out_host: (len(inputs), 1 + nparams) float64
+        host tensor (pinned) that receives each step's loss and gradient.
+        Returns once everything is enqueued; synchronise before reading."""
+        step = self.step
+        comp = torch.cuda.current_stream(step.device)
+        step._set_params(params)
+        for b in range(2):
+            self.free[b].record(comp)
+
+        def feed(k):
+            b = k % 2
+            self.copy.wait_event(self.free[b])  # the graph that last read buffer b is done
+            with torch.cuda.stream(self.copy):
+                self.pos[b].copy_(inputs[k][0], non_blocking=True)
+                self.tgt[b].copy_(inputs[k][1], non_blocking=True)
+                self.copied[b].record(self.copy)
+
+        n = len(inputs)
+        if n:
+            feed(0)
+        for k in range(n):
+            if k + 1 < n:
+                feed(k + 1)
+            b = k % 2
+            comp.wait_event(self.copied[b])
+            self.graphs[b].replay()
+            self.free[b].record(comp)
+            out_host[k].copy_(step.out, non_blocking=True)

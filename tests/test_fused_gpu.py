@@ -222,3 +222,25 @@ def test_fused_rejects_bad_arguments():
         f(pos, np.zeros(13), torch.zeros((16, 16, 16), device="cuda"))
     with pytest.raises(_lib.JLDError):
         FusedLDL((16, 16, 15), 10.0, 100)
+
+
+def test_host_feed_matches_eager_steps():
+    # three steps fed from pinned host memory (copies overlapped with the
+    # previous step) give each step's own loss and gradient
+    from jerald_gb300.ldl import FusedLDL, HostFeed
+    n, box = 32, 100.0
+    cases = [_case(n, box, "sm", True, s) for s in (41, 42, 43)]
+    p = cases[0][1]
+    f = FusedLDL(n, box, len(cases[0][0]), nstep=2, kind="sm", L1=True)
+    feed = HostFeed(f)
+    inputs = [(torch.from_numpy(X.astype(np.float32)).pin_memory(), torch.from_numpy(t).pin_memory())
+              for X, _, t, _, _ in cases]
+    out = torch.zeros((3, 1 + f.nparams), dtype=torch.float64).pin_memory()
+    feed.run(inputs, p, out)
+    torch.cuda.synchronize()
+    for k, (ph, th) in enumerate(inputs):
+        lo, go = f(ph.cuda(), p, th.cuda())
+        torch.cuda.synchronize()
+        assert abs(float(out[k, 0]) - float(lo)) <= 1e-6 * abs(float(lo))
+        assert _rel(out[k, 1:].numpy(), go.cpu().numpy()).max() < 1e-4
+    assert float(out[0, 0]) != float(out[1, 0])
