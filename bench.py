@@ -199,9 +199,11 @@ def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int
     """Times the oracle's 2-layer fwd+grad at n_sample^3 (clustered recipe)."""
     from jerald_gb300 import synth
     from oracle import fft as offt
+    from oracle import cic as ocic
     from oracle.ldl import LDLOracle
     threads = threads or os.cpu_count() or 1
     offt.set_workers(threads)
+    ocic.set_threads(threads)
     box = 100.0 * n_sample / 64
     X = synth.clustered(n_sample, box, seed=0).astype(np.float64)
     p = synth.default_params(2)
@@ -218,7 +220,8 @@ def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int
     value = (1.0 / dt) * n_part_sample / n_part_full
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"oracle 2-layer fwd+grad at {n_sample}^3 ({n_part_sample} particles, "
-                      f"{dt:.2f} s/step; CIC loops single-threaded C, FFT pocketfft with {threads} workers), "
+                      f"{dt:.2f} s/step; CIC loops in C over {threads} particle ranges on {threads} threads, "
+                      f"FFT pocketfft with {threads} workers), "
                       f"scaled by particle count to {n_full}^3"}
 
 

@@ -15,6 +15,32 @@ import numpy as np
 from .build import build
 
 _lib = None
+_THREADS = 1
+
+
+def set_threads(n: int) -> None:
+    """Host threads for the particle loops (1 = the reference's serial loops,
+    the default the tests use).  With n > 1 the particles are split into n
+    contiguous ranges run concurrently (the C calls release the GIL): gathers
+    are unchanged bit for bit; each range paints into its own mesh and the
+    meshes are summed in range order, as n ranks' slabs would be, which
+    changes only the summation order of the deposits."""
+    global _THREADS
+    _THREADS = max(1, int(n))
+
+
+def _ranges(n: int):
+    k = _THREADS if n >= 4096 * _THREADS else 1
+    edges = np.linspace(0, n, k + 1).astype(np.int64)
+    return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:])]
+
+
+def _pool_map(fn, ranges):
+    if len(ranges) == 1:
+        return [fn(*ranges[0])]
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(len(ranges)) as ex:
+        return list(ex.map(lambda r: fn(*r), ranges))
 
 
 def _load():
@@ -68,8 +94,16 @@ def paint(pos_mesh: np.ndarray, mass, nmesh) -> np.ndarray:
     dt = pos_mesh.dtype
     m = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, dtype=dt), (len(pos_mesh),)))
     nm = _nm(nmesh)
-    out = np.empty(tuple(int(v) for v in nm), dtype=dt)
-    getattr(_load(), f"orc_paint_{_sfx(pos_mesh)}")(_p(pos_mesh), ct.c_int64(len(pos_mesh)), _p(m), _p(nm), _p(out))
+    fn = getattr(_load(), f"orc_paint_{_sfx(pos_mesh)}")
+
+    def part(a, b):
+        out = np.empty(tuple(int(v) for v in nm), dtype=dt)
+        fn(_p(pos_mesh[a:]), ct.c_int64(b - a), _p(m[a:]), _p(nm), _p(out))
+        return out
+    meshes = _pool_map(part, _ranges(len(pos_mesh)))
+    out = meshes[0]
+    for extra in meshes[1:]:
+        out += extra
     return out
 
 
@@ -92,8 +126,9 @@ def readout(pos_mesh: np.ndarray, field: np.ndarray, nmesh, box, vjpdim: int = -
     nm = _nm(nmesh)
     b = np.ascontiguousarray(np.asarray(box, dtype=dt).reshape(3))
     out = np.empty(len(pos_mesh), dtype=dt)
-    getattr(_load(), f"orc_readout_{_sfx(pos_mesh)}")(_p(pos_mesh), ct.c_int64(len(pos_mesh)), _p(f), _p(nm), _p(b),
-                                                       ct.c_int(int(vjpdim)), _p(out))
+    fn = getattr(_load(), f"orc_readout_{_sfx(pos_mesh)}")
+    _pool_map(lambda a, e: fn(_p(pos_mesh[a:]), ct.c_int64(e - a), _p(f), _p(nm), _p(b), ct.c_int(int(vjpdim)),
+                              _p(out[a:])), _ranges(len(pos_mesh)))
     return out
 
 
@@ -105,6 +140,7 @@ def readout3d(pos_mesh: np.ndarray, field: np.ndarray, nmesh, box, vjp: bool) ->
     nm = _nm(nmesh)
     b = np.ascontiguousarray(np.asarray(box, dtype=dt).reshape(3))
     out = np.empty((len(pos_mesh), 3), dtype=dt)
-    getattr(_load(), f"orc_readout3d_{_sfx(pos_mesh)}")(_p(pos_mesh), ct.c_int64(len(pos_mesh)), _p(f), _p(nm), _p(b),
-                                                         ct.c_int(1 if vjp else 0), _p(out))
+    fn = getattr(_load(), f"orc_readout3d_{_sfx(pos_mesh)}")
+    _pool_map(lambda a, e: fn(_p(pos_mesh[a:]), ct.c_int64(e - a), _p(f), _p(nm), _p(b), ct.c_int(1 if vjp else 0),
+                              _p(out[a:])), _ranges(len(pos_mesh)))
     return out

@@ -102,21 +102,31 @@ def test_fused_positions_match_oracle_layers():
     assert np.abs(got - X1).max() < 1e-4 * max(disp, 1.0) + 2e-5 * box
 
 
-def test_fused_matches_plain_primitives():
+@pytest.mark.parametrize("L1", [True, False])
+def test_fused_matches_plain_primitives(L1):
+    # Both paths in FP32.  With the L1 loss the gradient depends on
+    # sign(F - t) per cell: rounding-level differences between the two paths
+    # flip a few cells (each moves d/db by 2/Npix), so the L1 case compares
+    # the loss and the gradient norm-wise; the smooth L2 case compares every
+    # gradient component.
     from jerald_gb300.model import JERALDModel
     from jerald_gb300.pmesh import PMesh
     n, box = 64, 200.0
-    X, p, tgt, o, _ = _case(n, box, "sm", True, 9, rms=1.0)
+    X, p, tgt, o, _ = _case(n, box, "sm", L1, 9, rms=1.0)
     pos = torch.from_numpy(X.astype(np.float32)).cuda()
     t = torch.from_numpy(tgt).cuda()
     pm = PMesh(n, box, dtype=torch.float32)
-    model = JERALDModel(pos, t, pm, Nstep=2, kind="sm")
+    model = JERALDModel(pos, t, pm, Nstep=2, kind="sm", L1=L1)
     lp, gp = model.loss_and_grad(torch.from_numpy(p.astype(np.float32)))
-    f = _fused(n, box, len(X), "sm", True, "reference")
+    f = _fused(n, box, len(X), "sm", L1, "reference")
     lf, gf = f(pos, p, t)
     torch.cuda.synchronize()
     assert abs(float(lf) - float(lp)) <= 2e-5 * abs(float(lp))
-    assert _rel(gf.cpu().numpy(), gp.cpu().numpy()).max() < 5e-3
+    gf, gp = gf.cpu().numpy(), gp.cpu().numpy().astype(np.float64)
+    if L1:
+        assert np.linalg.norm(gf - gp) / np.linalg.norm(gp) < 5e-2
+    else:
+        assert _rel(gf, gp).max() < 5e-3
 
 
 def test_tiled_scatters_match_atomic_scatters_clustered():
