@@ -237,8 +237,9 @@ static int ldl_step(const StepArgs& a) {
   ZPipeGeom zr2c, zc2r3, zadj, zr2c3;
   if (a.use_pipe) {
     zr2c = zpipe_geom(rows, h, 1, (size_t)h * 8);
-    zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8);
-    zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8);
+    // ~100 registers per thread: 192 / 128-thread CTAs keep 3-5 resident per SM
+    zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8, 110 * 1024, 192);
+    zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8, 110 * 1024, 128);
     zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16);
   }
   // the generic kernels then only cover the nyq plane

@@ -117,7 +117,10 @@ struct ZPipeGeom {
 
 // slot_row = staging bytes per row of the tile (all meshes), cap = shared
 // memory limit.
-inline ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, size_t slot_row, size_t cap = 110 * 1024) {
+// max_thr caps the CTA size for kernels whose register count would
+// otherwise leave one CTA per SM (smaller tiles, more resident CTAs).
+inline ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, size_t slot_row, size_t cap = 110 * 1024,
+                            int max_thr = 512) {
   ZPipeGeom z;
   if (h < 16 || h > 2048 || (h & (h - 1))) return z;
   const int ldw = h + h / 16;
@@ -125,7 +128,7 @@ inline ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, size_t slot_row, size_
     const int lines = nin * R;
     const int64_t thr = (int64_t)lines * h / 16;
     const size_t smem = (size_t)R * slot_row + (size_t)lines * ldw * 8 + 16;
-    if (thr > 512 || rows % R || smem > cap) continue;
+    if (thr > max_thr || rows % R || smem > cap) continue;
     if (thr < 32) return z;
     z.ok = true;
     z.zt.R = R;
