@@ -60,9 +60,11 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 
 // ---------------------------------------------------------------------------
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
-// Warps walk 16 x 2 particle tasks (PairWalk, row-length hint nz; all
-// lanes stay in the loop for the shuffles) and merge the stencil faces
-// their neighbours share before the atomics (pairing_flags).
+// Warps walk 32 consecutive particles at a time (all lanes stay in the loop
+// for the shuffles); lanes whose stencils share a z face merge it before
+// the atomics (zpair32_flags).  The 16 x 2 layout with y pairing as well
+// (pairing_flags) measured slower here: a scalar atomic costs less than
+// the extra shuffles and ballots.
 // Occupancy matters more than registers here (latency-bound loads and
 // atomics): six CTAs of 256 threads per SM in single precision.
 template <typename T, bool BOX>
@@ -70,9 +72,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;
-  for (PairWalk pw(n, g.nz); pw.more(); pw.next()) {
-    const int64_t p = pw.particle();
-    const bool live = p >= 0;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const int64_t p = base + lane;
+    const bool live = p < n;
     T q[3] = {T(0), T(0), T(0)};
     T m = T(0);
     if (live) {
@@ -90,17 +94,11 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
       int bits = corner_axis_bits(k);
       w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
     }
-    const Pairing pr = pairing_flags(live ? pair_key(c, g) : kNoPair, (uint32_t)g.sy);
+    const Pairing pr = zpair32_flags(live ? pair_key(c, g) : kNoPair);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const T t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
       if (pr.tz) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
-    }
-    {
-      const T t2 = __shfl_up_sync(full, w[2], 16), t4 = __shfl_up_sync(full, w[4], 16);
-      const T t6 = __shfl_up_sync(full, w[6], 16), t7 = __shfl_up_sync(full, w[7], 16);
-      if (pr.ty) { w[0] = add_rn(w[0], t2); w[1] = add_rn(w[1], t4); }
-      if (pr.thz) { w[3] = add_rn(w[3], t6); w[5] = add_rn(w[5], t7); }
     }
     if (live) {
 #pragma unroll

@@ -234,6 +234,21 @@ __device__ __forceinline__ Pairing pairing_flags(uint32_t key, uint32_t sy) {
   return p;
 }
 
+// z pairing only, for 32 consecutive particles per warp (lane l absorbs
+// lane l-1's upper-z face): fewer shuffles and ballots than the 16 x 2
+// layout, for scatters whose atomics are cheap next to those instructions.
+__device__ __forceinline__ Pairing zpair32_flags(uint32_t key) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t kz = __shfl_up_sync(full, key, 1);
+  Pairing p;
+  p.tz = lane > 0 && key != kNoPair && kz != kNoPair && key == kz + 1u;
+  const unsigned bz = __ballot_sync(full, p.tz);
+  p.gz = lane < 31 && ((bz >> (lane + 1)) & 1u);
+  p.ty = p.gy = p.thz = p.ghz = false;
+  return p;
+}
+
 // Reference corner order k -> axis bits (x = bit 0): the upper-z corners
 // k = 3, 5, 6, 7 pair with the lower-z corners k = 0, 1, 2, 4.
 __device__ __forceinline__ constexpr int zpair_hi(int j) { return j == 0 ? 3 : j == 1 ? 5 : j == 2 ? 6 : 7; }
