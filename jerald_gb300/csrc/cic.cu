@@ -190,26 +190,35 @@ template <typename T, bool BOX>
 __global__ void __launch_bounds__(256)
 readout_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ field, Grid3 g,
                int vjpdim, T dweight, T* __restrict__ out) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    T q[3];
-    load_pos<T, BOX>(src, p, q);
-    Corners<T> c;
-    cic_corners(q, g, c);
-    T lo[3], hi[3];
+  // Two particles per iteration (p and p + S): their sixteen gathers are in
+  // flight together, which matters for this latency-bound loop.
+  const int64_t S = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < n; p0 += 2 * S) {
+    const int64_t pp[2] = {p0, p0 + S < n ? p0 + S : p0};
+    Corners<T> c[2];
+    T lo[2][3], hi[2][3], v[2][8];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
-    if (vjpdim >= 0) { hi[vjpdim] = dweight; lo[vjpdim] = -dweight; }
-    T acc = T(0);
+    for (int i = 0; i < 2; ++i) {
+      T q[3];
+      load_pos<T, BOX>(src, pp[i], q);
+      cic_corners(q, g, c[i]);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      int bits = corner_axis_bits(k);
-      T v = __ldg(field + corner_offset(c, bits, g));
-      T t = mul_rn(mul_rn(corner_weight(lo, hi, bits), v),
-                   corner_ok(c, bits) ? T(1) : T(0));
-      acc = (k == 0) ? t : add_rn(acc, t);
+      for (int a = 0; a < 3; ++a) { hi[i][a] = c[i].d[a]; lo[i][a] = sub_rn(T(1), c[i].d[a]); }
+      if (vjpdim >= 0) { hi[i][vjpdim] = dweight; lo[i][vjpdim] = -dweight; }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[i][k] = __ldg(field + corner_offset(c[i], corner_axis_bits(k), g));
     }
-    out[p] = acc;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int bits = corner_axis_bits(k);
+        T t = mul_rn(mul_rn(corner_weight(lo[i], hi[i], bits), v[i][k]), corner_ok(c[i], bits) ? T(1) : T(0));
+        acc = (k == 0) ? t : add_rn(acc, t);
+      }
+      if (i == 0 || p0 + S < n) out[pp[i]] = acc;
+    }
   }
 }
 
