@@ -426,38 +426,26 @@ __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int
 
 // X' = X + readout of the float4 force mesh (three channels, the reference's
 // per-channel summation order).
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 6)
 update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
               const float4* __restrict__ g4, float* __restrict__ Xn) {
-  // Two particles per iteration (p and p + S) keep sixteen gathers in flight.
-  const int64_t S = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 < n; p0 += 2 * S) {
-    const int64_t pp[2] = {p0, p0 + S < n ? p0 + S : p0};
-    Corners<float> c[2];
-    float lo[2][3], hi[2][3];
-    float4 v[2][8];
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    Corners<float> c;
+    float lo[3], hi[3];
+    particle_setup(X, p, bg, g, c, lo, hi);
+    float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      particle_setup(X, pp[i], bg, g, c[i], lo[i], hi[i]);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) v[i][k] = __ldg(g4 + corner_offset(c[i], corner_axis_bits(k), g));
+    for (int k = 0; k < 8; ++k) {
+      int bits = corner_axis_bits(k);
+      float4 v = __ldg(g4 + corner_offset(c, bits, g));
+      float w = corner_ok(c, bits) ? wprod(lo, hi, bits) : 0.f;
+      float t0 = __fmul_rn(w, v.x), t1 = __fmul_rn(w, v.y), t2 = __fmul_rn(w, v.z);
+      if (k == 0) { acc[0] = t0; acc[1] = t1; acc[2] = t2; }
+      else { acc[0] = __fadd_rn(acc[0], t0); acc[1] = __fadd_rn(acc[1], t1); acc[2] = __fadd_rn(acc[2], t2); }
     }
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int bits = corner_axis_bits(k);
-        const float w = corner_ok(c[i], bits) ? wprod(lo[i], hi[i], bits) : 0.f;
-        const float t0 = __fmul_rn(w, v[i][k].x), t1 = __fmul_rn(w, v[i][k].y), t2 = __fmul_rn(w, v[i][k].z);
-        if (k == 0) { acc[0] = t0; acc[1] = t1; acc[2] = t2; }
-        else { acc[0] = __fadd_rn(acc[0], t0); acc[1] = __fadd_rn(acc[1], t1); acc[2] = __fadd_rn(acc[2], t2); }
-      }
-      if (i == 0 || p0 + S < n) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) Xn[3 * pp[i] + a] = __fadd_rn(__ldg(X + 3 * pp[i] + a), acc[a]);
-      }
-    }
+    for (int a = 0; a < 3; ++a) Xn[3 * p + a] = __fadd_rn(__ldg(X + 3 * p + a), acc[a]);
   }
 }
 
