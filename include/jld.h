@@ -65,6 +65,13 @@ enum {
 JLD_API const char* jld_version(void);
 JLD_API const char* jld_status_string(int status);
 JLD_API const char* jld_last_error(void);
+/* Copies `bytes` from page-locked host memory to device memory with a  */
+/* kernel that reads the host buffer directly (over NVLink-C2C on a GB300 */
+/* node) instead of the copy engines; `ctas` CTAs of 512 threads (<= 0:   */
+/* two per SM).  Both pointers 16-byte aligned.  Stream-ordered.  No      */
+/* counterpart in the reference (host-feed helper).                       */
+JLD_API int jld_copy_from_host(jld_stream_t stream, void* dst, const void* src_host, size_t bytes,
+                               int32_t ctas);
 /* Number of kernel nodes in a captured CUDA graph (cudaGraph_t passed as */
 /* void*): the kernel launches one replay issues.  No counterpart in the  */
 /* reference (measurement helper).                                        */

@@ -63,6 +63,7 @@ _SIGS = {
     "jld_ldl_error_word_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
     "jld_ldl_order_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
     "jld_graph_kernel_nodes": [_c_void_p, _c_void_p],
+    "jld_copy_from_host": [_c_void_p, _c_void_p, _c_void_p, _size, _i32],
     "jld_fft_pipe_status": [_c_void_p, _i32],
 }
 _RESTYPES = {

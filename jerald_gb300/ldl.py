@@ -184,9 +184,11 @@ class HostFeed:
     """Runs a FusedLDL from host-resident inputs, one step per input pair,
     with the host-to-device copies of step k+1 overlapped with the compute
     of step k: two device input buffers with one captured graph each, a copy
-    stream and events.  Every step's positions and target are copied from
-    (pinned) host memory and its loss and gradient are read back; only the
-    order of the copies changes, not their amount.
+    stream and events.  Page-locked inputs are streamed in by a small kernel
+    that reads host memory directly (jld_copy_from_host); others go through
+    copy_.  Every step's positions and target are copied and its loss and
+    gradient are read back; only the order of the copies changes, not their
+    amount.
     """
 
     def __init__(self, step: FusedLDL, mask=None):
@@ -199,6 +201,7 @@ class HostFeed:
         self.mask = mask
         self.graphs = [step.capture_graph(self.pos[b], self.tgt[b], mask) for b in range(2)]
         self.copy = torch.cuda.Stream(dev)
+        self.ctas = 16  # enough to saturate the host link; leaves the SMs to the step
         self.copied = [torch.cuda.Event() for _ in range(2)]
         self.free = [torch.cuda.Event() for _ in range(2)]
 
@@ -213,12 +216,24 @@ class HostFeed:
         for b in range(2):
             self.free[b].record(comp)
 
+        cs = ct.c_void_p(self.copy.cuda_stream)
+
+        def put(dst: torch.Tensor, src: torch.Tensor) -> None:
+            nbytes = dst.numel() * dst.element_size()
+            if (src.is_pinned() and src.is_contiguous() and src.numel() == dst.numel()
+                    and src.dtype == dst.dtype and src.data_ptr() % 16 == 0):
+                # a few CTAs read the page-locked buffer directly (NVLink-C2C)
+                _lib.call("jld_copy_from_host", cs, ct.c_void_p(dst.data_ptr()), ct.c_void_p(src.data_ptr()),
+                          nbytes, self.ctas)
+            else:
+                dst.copy_(src, non_blocking=True)
+
         def feed(k):
             b = k % 2
             self.copy.wait_event(self.free[b])  # the graph that last read buffer b is done
             with torch.cuda.stream(self.copy):
-                self.pos[b].copy_(inputs[k][0], non_blocking=True)
-                self.tgt[b].copy_(inputs[k][1], non_blocking=True)
+                put(self.pos[b], inputs[k][0])
+                put(self.tgt[b], inputs[k][1])
                 self.copied[b].record(self.copy)
 
         n = len(inputs)

@@ -342,3 +342,17 @@ def test_fft_roundtrip_large(jl):
     jl.call("jld_pifft_c_f32", _st(), _p(spec), *nm, _p(y), _p(ws), ws.numel())
     err = (y / x.numel() - x).abs().max().item()
     assert err < 2e-5
+
+
+@pytest.mark.parametrize("nbytes", [16, 1000003, 64 << 20])
+def test_copy_from_host_kernel(jl, nbytes):
+    # the host-feed copy kernel reproduces the page-locked source exactly,
+    # including a tail that is not a whole 16-byte word
+    src = torch.randint(0, 256, (nbytes,), dtype=torch.uint8).pin_memory()
+    dst = torch.zeros(nbytes + 16, dtype=torch.uint8, device="cuda")
+    jl.call("jld_copy_from_host", _st(), _p(dst), _p(src), nbytes, 16)
+    torch.cuda.synchronize()
+    assert torch.equal(dst[:nbytes].cpu(), src)
+    assert int(dst[nbytes:].sum()) == 0
+    with pytest.raises(jl.JLDError):  # pageable source is rejected
+        jl.call("jld_copy_from_host", _st(), _p(dst), _p(torch.empty(64, dtype=torch.uint8)), 64, 16)
