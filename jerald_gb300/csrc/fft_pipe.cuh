@@ -241,6 +241,34 @@ template <> struct P2For<512> { using type = P2<16, 16, 2>; };
 template <> struct P2For<1024> { using type = P2<16, 16, 4>; };
 template <> struct P2For<2048> { using type = P2<16, 16, 8>; };
 
+// Radix-8 family: 8 values per thread per line, so a kernel can stay under
+// 64 registers and keep twice the warps resident (used by the x passes,
+// whose three transforms per tile otherwise hold 128 registers).
+template <int N> struct P2For8;
+template <> struct P2For8<16> { using type = P2<8, 2>; };
+template <> struct P2For8<32> { using type = P2<8, 4>; };
+template <> struct P2For8<64> { using type = P2<8, 8>; };
+template <> struct P2For8<128> { using type = P2<8, 8, 2>; };
+template <> struct P2For8<256> { using type = P2<8, 8, 4>; };
+template <> struct P2For8<512> { using type = P2<8, 8, 8>; };
+template <> struct P2For8<1024> { using type = P2<8, 8, 8, 2>; };
+template <> struct P2For8<2048> { using type = P2<8, 8, 8, 4>; };
+
+template <class F>
+inline int with_p2_8(int n, F&& body) {
+  switch (n) {
+    case 16: return body(P2For8<16>::type{});
+    case 32: return body(P2For8<32>::type{});
+    case 64: return body(P2For8<64>::type{});
+    case 128: return body(P2For8<128>::type{});
+    case 256: return body(P2For8<256>::type{});
+    case 512: return body(P2For8<512>::type{});
+    case 1024: return body(P2For8<1024>::type{});
+    case 2048: return body(P2For8<2048>::type{});
+    default: return -1;
+  }
+}
+
 // Calls body(P2For<N>::type{}) for a supported power of two; returns -1 if
 // n has no pipelined schedule.
 template <class F>

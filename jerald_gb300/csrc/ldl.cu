@@ -232,7 +232,12 @@ static int ldl_step(const StepArgs& a) {
   int* err = (int*)(ws + L.off_err);
   JLD_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int) * 4, st));
   const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0), py1 = pipe_geom(nx, ny, h, 1, 1);
-  const PipeGeom px1 = pipe_geom(nx, ny, h, 0, 1);
+  const PipeGeom px16 = pipe_geom(nx, ny, h, 0, 1);
+  // x passes: radix-8 schedules at <= 64 registers (twice the warps per SM)
+  // where the tile fits, else the radix-16 ones
+  const PipeGeom px8 = pipe_geom(nx, ny, h, 0, 1, 8, 64);
+  const PipeGeom& px1 = px8.ok ? px8 : px16;
+  auto with_x = [&](auto&& body) { return px8.ok ? with_p2_8(nx, body) : with_p2(nx, body); };
   const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
   ZPipeGeom zr2c, zc2r3, zadj, zr2c3;
   if (a.use_pipe) {
@@ -309,7 +314,7 @@ static int ldl_step(const StepArgs& a) {
     if (pipe) {
       CUtensorMap mA;
       if ((s = xmap(&mA, W[0], px1))) return s;
-      s = with_p2(nx, [&](auto sch) {
+      s = with_x([&](auto sch) {
         using Sch = decltype(sch);
         int r = ensure_smem(xfilt_pipe_kernel<Sch>, px1.smem);
         if (r) return r;
@@ -491,7 +496,7 @@ static int ldl_step(const StepArgs& a) {
     if (pipe) {
       CUtensorMap m0, m1, m2;
       if ((s = xmap(&m0, W[0], px1)) || (s = xmap(&m1, W[3], px1)) || (s = xmap(&m2, S_l, px1))) return s;
-      s = with_p2(nx, [&](auto sch) {
+      s = with_x([&](auto sch) {
         using Sch = decltype(sch);
         int r = ensure_smem(xbwd_pipe_kernel<Sch>, px1.smem);
         if (r) return r;

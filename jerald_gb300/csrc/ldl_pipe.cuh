@@ -21,7 +21,7 @@ __device__ __forceinline__ void xcols(const SGeom& g, int t, int* ky, int* kz, i
 // Forward x pass: S = FFT_x(A) (kept for the adjoint), P = 1e-2 alpha G S / Nc,
 // T0 = iFFT_x(P), T1 = iFFT_x(-i c_x P).
 template <class Sch>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, const float* __restrict__ params,
                   int kind, float scale, float2* __restrict__ S, float2* __restrict__ T0,
                   float2* __restrict__ T1, const float2* __restrict__ tw, int* err) {
@@ -191,7 +191,7 @@ yfwd_comb_pipe_kernel(const __grid_constant__ CUtensorMap mAx, const __grid_cons
 // Adjoint x pass with the parameter-gradient reductions; items per tile:
 // Bx, D, S.  Partials per block: [d alpha, d kh, d kl, d nu].
 template <class Sch>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant__ CUtensorMap mD,
                  const __grid_constant__ CUtensorMap mS, SGeom g, KTables kt, const float* __restrict__ params,
                  int kind, int mode, float scale, float2* __restrict__ Vout, double* __restrict__ partials,

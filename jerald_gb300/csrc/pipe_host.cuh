@@ -70,7 +70,9 @@ struct PipeGeom {
   size_t smem = 0;
 };
 
-inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc) {
+// E = values per thread per line of the schedule (16: P2For, 8: P2For8);
+// regs = registers per thread the kernel is built for.
+inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, int regs = 128) {
   PipeGeom p;
   const int lines = ax == 1 ? ny : nx;
   if (lines < 16 || lines > 2048 || (lines & (lines - 1)) || h < 2 || (h & 1)) return p;
@@ -79,7 +81,7 @@ inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc) {
   // FFT stages; a second CTA keeps the SM busy meanwhile), else the widest
   // that fits alone.
   auto smem_of = [&](int c) { return (size_t)lines * c * 8 * (2 + nacc) + 64; };
-  auto fits = [&](int c, size_t cap) { return c * lines / 16 <= 512 && h % c == 0 && smem_of(c) <= cap; };
+  auto fits = [&](int c, size_t cap) { return c * lines / E <= 512 && h % c == 0 && smem_of(c) <= cap; };
   int cols = 16;
   while (cols >= 4 && !fits(cols, 112 * 1024)) cols >>= 1;
   if (cols < 4) {
@@ -94,10 +96,10 @@ inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc) {
   g.lines = lines;
   g.ntiles = (int)(((int64_t)(ax == 1 ? nx : ny) * h) / cols);
   g.es = ax == 1 ? h : (int64_t)ny * h;
-  p.nthr = cols * lines / 16;
+  p.nthr = cols * lines / E;
   p.smem = smem_of(cols);
-  // resident CTAs per SM: shared memory, registers (<= 128 per thread) and threads
-  const int per_sm = std::max(1, std::min({(int)((227 * 1024) / (p.smem + 1024)), 65536 / (p.nthr * 128),
+  // resident CTAs per SM: shared memory, registers and threads
+  const int per_sm = std::max(1, std::min({(int)((227 * 1024) / (p.smem + 1024)), 65536 / (p.nthr * regs),
                                            2048 / p.nthr, 32}));
   p.grid = (int)std::min<int64_t>(g.ntiles, (int64_t)per_sm * sm_count());
   p.ok = true;

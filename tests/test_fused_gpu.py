@@ -196,7 +196,7 @@ def test_pipelined_passes_match_generic_passes(n):
     assert float((xa - xb).abs().max()) < 1e-4
 
 
-@pytest.mark.parametrize("nm", [(512, 16, 32), (16, 512, 64), (64, 32, 1024)])
+@pytest.mark.parametrize("nm", [(512, 16, 32), (16, 512, 64), (64, 32, 1024), (1024, 16, 32)])
 def test_pipelined_passes_match_generic_non_cubic(nm):
     # long x / y / z lines: narrower pipelined tiles (two CTAs per SM) and
     # few rows per z tile
