@@ -227,3 +227,68 @@ class LDLOracle:
             out[i] = (self.forward(p1, X, target, nstep, mask) -
                       self.forward(p0, X, target, nstep, mask)) / (2 * step)
         return out
+
+
+def model_loss(nmesh, box, kind, params, X, target, nstep, starmap=None, n=0, index=1.0, L1=None,
+               field2=None, mask=None, maskvalid=None):
+    """FP64 forward of model.py's full loss for every kind and option, by the
+    oracle primitives: kinds "dm", "sm" and "HI" (potential_gradient_HI,
+    model.py:213-247, with the star-map source; HI final map model.py:313-336),
+    the field exponent `index` and second field (model.py:368-372), the
+    residual smoothing |k|^-n + 1 without c2f (model.py:376-381), training
+    and validation masks (model.py:384-390, 454-465).  Returns (loss, lossv)
+    (lossv = 0 without a validation mask).  Forward only: gradients of the
+    options are checked against its central differences."""
+    o = LDLOracle(nmesh, box, kind="dm" if kind == "dm" else "sm")
+    N = o.nmesh
+    k = o.knorm
+    params = np.asarray(params, dtype=np.float64)
+    X = np.asarray(X, dtype=np.float64).copy()
+    relu = lambda v: np.where(v > 1e-12, v, 1e-12)  # noqa: E731  (model.py:55-57)
+    r2c = lambda f: pfft(f) / o.ncell                 # noqa: E731  (pmesh.py:112)
+    c2r = lambda fk: pifft(fk, N)                     # noqa: E731
+    fact = o.ncell / len(X)
+    npot = 10 if kind == "HI" else 5
+    for layer in range(nstep):
+        p = params[npot * layer: npot * (layer + 1)]
+        Xm = o.mesh_pos(X)
+        rho = cic.paint(Xm, 1.0, N) * fact
+        if kind == "HI":
+            a1, g1, kh1, kl1, nu1, a2, g2, kh2, kl2, nu2 = p
+            G1 = -np.exp(-k ** 2 / kl1 ** 2 - kh1 ** 2 / k ** 2) * k ** nu1
+            G2 = np.exp(-k ** 2 / kl2 ** 2 - kh2 ** 2 / k ** 2) * k ** nu2
+            potk = 1e-3 * (a1 * G1 * r2c((rho + 1e-8) ** g1) + a2 * G2 * r2c(np.asarray(starmap) ** g2))
+        else:
+            a, g, kh, kl, nu = p
+            potk = 1e-2 * a * r2c((rho + 1e-8) ** g) * o.green(kh, kl, nu)
+        disp = [cic.readout(Xm, c2r(-1j * o.coeff[d] * potk), N, o.box) for d in range(3)]
+        X = X + np.stack(disp, axis=-1)
+    rho = cic.paint(o.mesh_pos(X), 1.0, N) * fact
+    q = params[npot * nstep:]
+    if kind == "HI":
+        mu, w, b, beta1, khi, kli, nui, beta2, gamma3, xi, eta, zs = q[:12]
+        sm = np.asarray(starmap, dtype=np.float64)
+        filt = np.exp(-k / kli - khi / k) * k ** nui + xi
+        depletion = relu(beta1 * c2r(r2c(sm) * filt) + eta) + beta2 * sm ** gamma3
+        F = relu(w * relu(rho + zs) ** mu - depletion + b)
+    elif kind == "sm":
+        mu, w, b = q[:3]
+        F = relu(w * (rho + 1e-8) ** mu + b)
+    else:
+        F = rho
+    F = F ** index
+    if field2 is not None:
+        F = F * field2
+    diff = F - target
+    if n > 0:
+        sk = np.where(k == 0, 1.0, k ** (-n) + 1.0)
+        diff = np.abs(c2r(r2c(diff) * sk))
+    else:
+        diff = np.abs(diff)
+    L1 = (kind != "dm") if L1 is None else L1
+
+    def red(m):
+        d = diff * m if m is not None else diff
+        npix = float(np.sum(m)) if m is not None else float(diff.size)
+        return float((np.sum(d) if L1 else np.sum(d * d)) / npix)
+    return red(mask), (red(maskvalid) if maskvalid is not None else 0.0)

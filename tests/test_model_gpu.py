@@ -94,3 +94,68 @@ def test_losstest_replica_f64():
     assert abs(float(lossv) - lossv_o) <= 1e-11 * abs(lossv_o)
     l2, lv2, g = model.lossv_and_grad(torch.from_numpy(param))
     assert _rel(g.cpu().numpy(), g_o).max() < 1e-7
+
+
+def _hi_params(nstep):
+    # per layer (alpha1, gamma1, kh1, kl1, nu1, alpha2, gamma2, kh2, kl2, nu2),
+    # then (mu, w, b, beta1, khi, kli, nui, beta2, gamma3, xi, eta, zs)
+    layer = [0.5, 1.0, 0.5, 2.0, 1.0, 0.3, 0.8, 0.6, 1.5, 0.5]
+    final = [1.2, 1.0, 0.2, 0.3, 0.5, 2.0, 0.5, 0.1, 0.9, 0.05, 0.1, 0.5]
+    return np.array(layer * nstep + final, dtype=np.float64)
+
+
+@pytest.mark.parametrize("case", ["HI", "sm_smooth", "sm_index_field2_valid"])
+def test_plain_model_options_match_oracle_and_differences(case):
+    """The model.py options outside the fused step -- the HI kind with its
+    star map, residual smoothing |k|^-n + 1, the field exponent and second
+    field, the validation mask -- on the FP64 plain path: loss (and lossv)
+    against the oracle's forward, gradient against central differences of
+    that forward (exact adjoint convention, smooth L2 loss)."""
+    from jerald_gb300 import jaxpops_bind as jpo
+    from jerald_gb300 import synth
+    from jerald_gb300.model import JERALDModel
+    from jerald_gb300.pmesh import PMesh
+    from oracle.ldl import model_loss
+    n, box = 16, 100.0
+    rng = np.random.default_rng(11)
+    X = synth.zeldovich(n, box, 0.5, seed=12, dtype=np.float64)
+    tgt = rng.uniform(0.5, 1.5, (n,) * 3)
+    kw = dict(L1=False)
+    opts = {}
+    if case == "HI":
+        kind, p = "HI", _hi_params(2)
+        opts["starmap"] = np.exp(0.3 * rng.standard_normal((n,) * 3))
+    elif case == "sm_smooth":
+        kind, p = "sm", synth.default_params(2)
+        opts["n"] = 2
+    else:
+        kind, p = "sm", synth.default_params(2)
+        opts["index"] = 2.0
+        opts["field2"] = rng.uniform(0.8, 1.2, (n,) * 3)
+        opts["mask"] = rng.integers(0, 2, (n,) * 3).astype(np.float64)
+        opts["maskvalid"] = 1.0 - opts["mask"]
+    ref, refv = model_loss((n,) * 3, box, kind, p, X, tgt, 2, **kw, **opts)
+    dev = lambda a: torch.from_numpy(np.asarray(a, dtype=np.float64)).cuda() if a is not None else None  # noqa
+    pm = PMesh(n, box, dtype=torch.float64)
+    model = JERALDModel(dev(X), dev(tgt), pm, Nstep=2, kind=kind, L1=False, n=opts.get("n", 0),
+                        index=opts.get("index", 1.0), field2=dev(opts.get("field2")),
+                        masktrain=dev(opts.get("mask")), maskvalid=dev(opts.get("maskvalid")),
+                        starmap=dev(opts.get("starmap")))
+    jpo.set_fft_adjoint("true")
+    try:
+        loss, lossv, g = model.lossv_and_grad(torch.from_numpy(p))
+    finally:
+        jpo.set_fft_adjoint("reference")
+    assert abs(float(loss) - ref) <= 1e-10 * abs(ref)
+    if "maskvalid" in opts:
+        assert abs(float(lossv) - refv) <= 1e-10 * abs(refv)
+    g = g.cpu().numpy()
+    fd = np.zeros_like(p)
+    for i in range(len(p)):
+        h = 1e-5 * max(abs(p[i]), 1e-2)
+        pp, pm_ = p.copy(), p.copy()
+        pp[i] += h
+        pm_[i] -= h
+        fd[i] = (model_loss((n,) * 3, box, kind, pp, X, tgt, 2, **kw, **opts)[0]
+                 - model_loss((n,) * 3, box, kind, pm_, X, tgt, 2, **kw, **opts)[0]) / (2 * h)
+    assert np.linalg.norm(g - fd) / np.linalg.norm(fd) < 1e-4

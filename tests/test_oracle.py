@@ -169,3 +169,21 @@ def test_reference_rule_differs_only_in_alpha():
     others = [i for i in range(13) if i not in alpha]
     np.testing.assert_allclose(gr[others], gt[others], rtol=1e-12, atol=1e-18)
     assert np.all(np.abs(gr[alpha] - gt[alpha]) > 1e-3 * np.abs(gt[alpha]))
+
+
+def test_model_loss_matches_pipeline_forward():
+    # the general forward (all kinds and options) agrees with the pipeline
+    # the gradient oracle differentiates, where both apply
+    from jerald_gb300 import synth
+    from oracle.ldl import LDLOracle, model_loss
+    n, box = 16, 50.0
+    X = synth.zeldovich(n, box, 0.5, seed=7).astype(np.float64)
+    for kind in ("sm", "dm"):
+        p = synth.default_params(2)
+        if kind == "dm":
+            p = p[:10]
+        tgt = np.random.default_rng(1).uniform(0.5, 1.5, (n,) * 3)
+        o = LDLOracle((n,) * 3, box, kind=kind, L1=(kind == "sm"))
+        a = o.forward(p, X, tgt, 2)
+        b, _ = model_loss((n,) * 3, box, kind, p, X, tgt, 2)
+        assert abs(a - b) <= 1e-12 * abs(a)
