@@ -356,3 +356,29 @@ def test_copy_from_host_kernel(jl, nbytes):
     assert int(dst[nbytes:].sum()) == 0
     with pytest.raises(jl.JLDError):  # pageable source is rejected
         jl.call("jld_copy_from_host", _st(), _p(dst), _p(torch.empty(64, dtype=torch.uint8)), 64, 16)
+
+
+def test_c1_scale_ops_match_oracle(jl):
+    # the 256^3 validation configuration: clustered positions (1.85e7
+    # particles), cell keys and readout bit-exact, paint within 1e-5 of the
+    # mesh scale, all through the C ABI against the oracle's C loops
+    from jerald_gb300 import synth
+    n, box = 256, 400.0
+    nm, b3 = (n, n, n), (box, box, box)
+    pos = synth.clustered(n, box, seed=5).astype(np.float32)
+    q = cic.box_to_mesh(pos, b3, nm)
+    b = _box(b3, np.float32)
+    dpos = _cuda(pos)
+    keys = torch.empty(len(pos), dtype=torch.int32, device="cuda")
+    jl.call("jld_cell_keys_f32", _st(), _p(dpos), len(pos), *nm, b.ctypes.data_as(ct.c_void_p), _p(keys))
+    np.testing.assert_array_equal(keys.cpu().numpy(), cic.cell_keys(q, nm))
+    field = np.random.default_rng(6).standard_normal(nm).astype(np.float32)
+    out = torch.empty(len(pos), dtype=torch.float32, device="cuda")
+    jl.call("jld_preadout_box_f32", _st(), _p(dpos), len(pos), _p(_cuda(field)), *nm,
+            b.ctypes.data_as(ct.c_void_p), -1, _p(out))
+    np.testing.assert_array_equal(out.cpu().numpy(), cic.readout(q, field, nm, b3, -1))
+    mesh = torch.empty(nm, dtype=torch.float32, device="cuda")
+    jl.call("jld_ppaint_box_f32", _st(), _p(dpos), len(pos), None, ct.c_float(1.0), *nm,
+            b.ctypes.data_as(ct.c_void_p), _p(mesh))
+    ref = cic.paint(q, np.float32(1.0), nm)
+    assert np.abs(mesh.cpu().numpy() - ref).max() <= _paint_tol(np.float32, ref)
