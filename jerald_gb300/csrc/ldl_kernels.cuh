@@ -429,11 +429,25 @@ __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int
 __global__ void __launch_bounds__(256, 6)
 update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
               const float4* __restrict__ g4, float* __restrict__ Xn) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
+  // the next iteration's position is loaded one iteration ahead
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float nr[3] = {0.f, 0.f, 0.f};
+  if (p < n) { nr[0] = __ldg(X + 3 * p); nr[1] = __ldg(X + 3 * p + 1); nr[2] = __ldg(X + 3 * p + 2); }
+  for (; p < n; p += stride) {
+    const float r[3] = {nr[0], nr[1], nr[2]};
+    const int64_t pn = p + stride;
+    if (pn < n) { nr[0] = __ldg(X + 3 * pn); nr[1] = __ldg(X + 3 * pn + 1); nr[2] = __ldg(X + 3 * pn + 2); }
     Corners<float> c;
     float lo[3], hi[3];
-    particle_setup(X, p, bg, g, c, lo, hi);
+    {
+      float q[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) q[a] = box_to_mesh_fast(r[a], bg.box[a], bg.dw[a]);
+      cic_corners(q, g, c);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = __fsub_rn(1.f, c.d[a]); }
+    }
     float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -445,7 +459,7 @@ update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
       else { acc[0] = __fadd_rn(acc[0], t0); acc[1] = __fadd_rn(acc[1], t1); acc[2] = __fadd_rn(acc[2], t2); }
     }
 #pragma unroll
-    for (int a = 0; a < 3; ++a) Xn[3 * p + a] = __fadd_rn(__ldg(X + 3 * p + a), acc[a]);
+    for (int a = 0; a < 3; ++a) Xn[3 * p + a] = __fadd_rn(r[a], acc[a]);
   }
 }
 
