@@ -49,25 +49,6 @@ __device__ __forceinline__ void load_pos(const PosSrc<T>& s, int64_t p, T q[3]) 
   }
 }
 
-// The prelude alone, on positions already in registers.
-template <typename T, bool BOX>
-__device__ __forceinline__ void prelude_pos(const PosSrc<T>& s, const T r[3], T q[3]) {
-  if (BOX) {
-    if constexpr (sizeof(T) == 4) {
-      if (s.fast) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) q[a] = box_to_mesh_fast(r[a], s.box[a], s.inv[a]);
-        return;
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) q[a] = box_to_mesh(r[a], s.box[a], s.cell[a]);
-  } else {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) q[a] = r[a];
-  }
-}
-
 // Per-axis weights of corner `bits`: lower corner t = 1 - d, upper corner d.
 template <typename T>
 __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bits) {
@@ -93,29 +74,15 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // the next iteration's position and mass are loaded one iteration ahead
-  T nr[3] = {T(0), T(0), T(0)}, nm = T(0);
-  auto fetch = [&](int64_t b) {
-    const int64_t p = b + lane;
-    if (p < n) {
-      const T* a = src.pos + 3 * p;
-      nr[0] = __ldg(a); nr[1] = __ldg(a + 1); nr[2] = __ldg(a + 2);
-      nm = mass ? __ldg(mass + p) : mscalar;
-    } else {
-      nr[0] = nr[1] = nr[2] = T(0);
-      nm = T(0);
-    }
-  };
-  int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
-  if (base < n) fetch(base);
-  for (; base < n; base += stride) {
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
     const int64_t p = base + lane;
     const bool live = p < n;
-    const T r[3] = {nr[0], nr[1], nr[2]};
-    const T m = nm;
-    if (base + stride < n) fetch(base + stride);
-    T q[3];
-    prelude_pos<T, BOX>(src, r, q);
+    T q[3] = {T(0), T(0), T(0)};
+    T m = T(0);
+    if (live) {
+      load_pos<T, BOX>(src, p, q);
+      m = mass ? __ldg(mass + p) : mscalar;
+    }
     Corners<T> c;
     cic_corners(q, g, c);
     T lo[3], hi[3];
