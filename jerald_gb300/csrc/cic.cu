@@ -321,11 +321,12 @@ static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* ma
   PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
   src.fast = fast ? 1 : 0;
   const int block = 256;
-  unsigned grid = grid_for(nparts, block);
   if (method == 1) {
+    const unsigned grid = resident_grid(paint_warpagg_kernel<T, true>, nparts, block);
     if (box) paint_warpagg_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
     else paint_warpagg_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
   } else {
+    const unsigned grid = resident_grid(paint_kernel<T, true>, nparts, block);
     if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
     else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
   }
@@ -345,9 +346,8 @@ static int paint3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* m
   if (nparts == 0) return JLD_OK;
   PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
   const int block = 256;
-  unsigned grid = grid_for(nparts, block);
-  if (box) paint3_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, g, out);
-  else paint3_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, g, out);
+  if (box) paint3_kernel<T, true><<<resident_grid(paint3_kernel<T, true>, nparts, block), block, 0, st>>>(src, nparts, mass, g, out);
+  else paint3_kernel<T, false><<<resident_grid(paint3_kernel<T, false>, nparts, block), block, 0, st>>>(src, nparts, mass, g, out);
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;
 }
@@ -368,9 +368,8 @@ static int readout_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* 
   const int64_t nm[3] = {nx, ny, nz};
   T dweight = vjpdim >= 0 ? (T)((T)nm[vjpdim] / box[vjpdim]) : T(0);
   const int block = 256;
-  unsigned grid = grid_for(nparts, block);
-  if (boxpos) readout_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
-  else readout_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
+  if (boxpos) readout_kernel<T, true><<<resident_grid(readout_kernel<T, true>, nparts, block), block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
+  else readout_kernel<T, false><<<resident_grid(readout_kernel<T, false>, nparts, block), block, 0, st>>>(src, nparts, field, g, vjpdim, dweight, out);
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;
 }
@@ -391,9 +390,8 @@ static int readout3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T*
   const int64_t nm[3] = {nx, ny, nz};
   for (int a = 0; a < 3; ++a) dw[a] = (T)((T)nm[a] / box[a]);
   const int block = 256;
-  unsigned grid = grid_for(nparts, block);
-  if (boxpos) readout3_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
-  else readout3_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
+  if (boxpos) readout3_kernel<T, true><<<resident_grid(readout3_kernel<T, true>, nparts, block), block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
+  else readout3_kernel<T, false><<<resident_grid(readout3_kernel<T, false>, nparts, block), block, 0, st>>>(src, nparts, field, g, vjp, dw[0], dw[1], dw[2], out);
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;
 }
@@ -413,9 +411,8 @@ static int keys_impl(cudaStream_t st, const T* pos, int64_t nparts, int64_t nx, 
   Grid3 g = make_grid(nx, ny, nz);
   PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
   const int block = 256;
-  unsigned grid = grid_for(nparts, block);
-  if (box) keys_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, g, keys);
-  else keys_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, g, keys);
+  if (box) keys_kernel<T, true><<<resident_grid(keys_kernel<T, true>, nparts, block), block, 0, st>>>(src, nparts, g, keys);
+  else keys_kernel<T, false><<<resident_grid(keys_kernel<T, false>, nparts, block), block, 0, st>>>(src, nparts, g, keys);
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;
 }

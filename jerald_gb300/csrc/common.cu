@@ -37,6 +37,24 @@ int sm_count() {
   return n;
 }
 
+int resident_blocks_ptr(const void* func, int block, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<std::pair<const void*, int>, std::pair<int, size_t>>, int> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_pair(std::make_pair(func, dev), std::make_pair(block, smem));
+  auto it = done.find(key);
+  if (it != done.end()) return it->second;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, block, smem) != cudaSuccess || per_sm < 1) {
+    (void)cudaGetLastError();
+    per_sm = 1;
+  }
+  done[key] = per_sm;
+  return per_sm;
+}
+
 int ensure_smem_ptr(const void* func, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<const void*, int>, size_t> done;

@@ -47,6 +47,23 @@ inline unsigned grid_for(int64_t n, int block, int per_sm = 8) {
   return (unsigned)(need < cap ? need : cap);
 }
 
+// CTAs of `func` (a __global__ function) that fit on one SM at this block
+// size and dynamic shared memory (cached per device and configuration).
+int resident_blocks_ptr(const void* func, int block, size_t smem);
+
+// Grid of a grid-stride loop over n items that runs in exactly one wave:
+// every SM holds as many CTAs as fit (from the kernel's registers and shared
+// memory), never more CTAs than items need.  A grid of more CTAs than fit
+// runs a partial second wave in which most SMs idle, because every CTA of
+// a grid-stride loop carries the same amount of work.
+template <typename K>
+inline unsigned resident_grid(K* func, int64_t n, int block, size_t smem = 0) {
+  int64_t need = (n + block - 1) / block;
+  int64_t cap = (int64_t)sm_count() * resident_blocks_ptr((const void*)func, block, smem);
+  if (need < 1) need = 1;
+  return (unsigned)(need < cap ? need : cap);
+}
+
 // Unit-mass CIC paint of box-unit positions into `out` (zeroed first); the
 // same kernels as jld_ppaint_box_f32 (method 0 atomics, 1 warp-aggregated)
 // with the division-free prelude (box_to_mesh_fast).

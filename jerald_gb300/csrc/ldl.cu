@@ -168,7 +168,6 @@ static int ldl_step(const StepArgs& a) {
   double* npix = (double*)(ws + L.off_npix);
   const int64_t nyq_off = (int64_t)nx * ny * h;
   const int pblock = 256;
-  const unsigned pgrid = grid_for(a.N, pblock);
   float* Xs0 = (float*)(ws + L.off_xs0);
   const float* X0 = a.binned ? Xs0 : a.pos0;
   auto Xl = [&](int l) -> const float* { return l == 0 ? X0 : Xs + (size_t)3 * a.N * (l - 1); };
@@ -196,11 +195,11 @@ static int ldl_step(const StepArgs& a) {
     JLD_CUDA_TRY(cudaMemsetAsync(tcounts, 0, sizeof(int) * tg.ntiles(), st));
     int* keys = (int*)(ws + L.off_keys);
     int* perm = (int*)(ws + L.off_perm);
-    bin_count_kernel<<<pgrid, pblock, 0, st>>>(a.pos0, a.N, boxv, cellv, g, tg, keys, tcounts);
+    bin_count_kernel<<<resident_grid(bin_count_kernel, a.N, pblock), pblock, 0, st>>>(a.pos0, a.N, boxv, cellv, g, tg, keys, tcounts);
     JLD_LAUNCH_CHECK("bin_count_kernel");
     bin_scan_kernel<<<1, 1024, 0, st>>>(tcounts, tg.ntiles(), tstarts, tfill);
     JLD_LAUNCH_CHECK("bin_scan_kernel");
-    bin_scatter_kernel<<<pgrid, pblock, 0, st>>>(a.pos0, a.N, keys, tfill, Xs0, perm);
+    bin_scatter_kernel<<<resident_grid(bin_scatter_kernel, a.N, pblock), pblock, 0, st>>>(a.pos0, a.N, keys, tfill, Xs0, perm);
     JLD_LAUNCH_CHECK("bin_scatter_kernel");
   }
   const int cblock = 256;
@@ -397,7 +396,7 @@ static int ldl_step(const StepArgs& a) {
   for (int l = 0; l < a.nstep; ++l) {
     float4* g4_l = g4_of(l);
     if ((s = force_mesh(l, g4_l))) return s;
-    update_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
+    update_kernel<<<resident_grid(update_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
     JLD_LAUNCH_CHECK("update_kernel");
     if ((s = paint_into(Xl(l + 1), rho + (size_t)L.C * (l + 1)))) return s;  // the final map for l = nstep-1
   }
@@ -410,7 +409,7 @@ static int ldl_step(const StepArgs& a) {
   launch_finish(st, part, (int)cgrid, 4, 1, a.out, 0, npix);
   if (a.kind == 0) launch_finish(st, part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
   if (!fuse_adj) {
-    gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
+    gather_vjp_kernel<<<resident_grid(gather_vjp_kernel, a.N, pblock), pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
     JLD_LAUNCH_CHECK("gather_vjp_kernel");
   }
 
@@ -439,9 +438,9 @@ static int ldl_step(const StepArgs& a) {
       // the first layer's input positions are data: scatter only
       const float* Xbp = (l == a.nstep - 1) ? nullptr : Xb;
       if (l > 0)
-        bwd_fused_kernel<true><<<pgrid, pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
+        bwd_fused_kernel<true><<<resident_grid(bwd_fused_kernel<true>, a.N, pblock), pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
       else
-        bwd_fused_kernel<false><<<pgrid, pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
+        bwd_fused_kernel<false><<<resident_grid(bwd_fused_kernel<false>, a.N, pblock), pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
       JLD_LAUNCH_CHECK("bwd_fused_kernel");
     }
     if (zr2c3.ok) {
@@ -551,7 +550,7 @@ static int ldl_step(const StepArgs& a) {
     JLD_LAUNCH_CHECK("zinv_adj_kernel");
     launch_finish(st, part, (int)adj_blocks, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
     if (l > 0 && !fuse_adj) {
-      gather_vjp_kernel<<<pgrid, pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
+      gather_vjp_kernel<<<resident_grid(gather_vjp_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
       JLD_LAUNCH_CHECK("gather_vjp_kernel");
     }
     std::swap(Xb, Xb2);

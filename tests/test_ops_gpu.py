@@ -185,6 +185,46 @@ def test_paint_methods_clustered(jl, method):
     assert np.abs(out.cpu().numpy() - ref).max() <= 2e-5 * scale
 
 
+def _paint_case(case):
+    """(positions, masses or None, mesh, box) of the paint-method cases: lattice
+    order (long z runs that the face pairing merges), clumps, both mixed,
+    meshes whose cells do not line up with the lattice, and edge stencils."""
+    from jerald_gb300 import synth
+    rng = np.random.default_rng(21)
+    if case == "exact_lattice":          # particles on cell corners: runs of 32
+        g = np.arange(32, dtype=np.float64) + 0.25
+        pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+        return pos, None, (32, 32, 32), (32.0, 32.0, 32.0)
+    if case.startswith("lattice"):
+        nm = {"lattice": (32, 32, 32), "lattice_nz34": (32, 32, 34), "lattice_nz33": (32, 32, 33)}[case]
+        pos = synth.zeldovich(32, 32.0, 0.7, seed=5)
+        return pos, rng.uniform(0.5, 1.5, len(pos)).astype(np.float32), nm, (32.0, 32.0, 32.0)
+    if case == "mixed":
+        pos = synth.clustered(16, 24.0, seed=3, extra_frac=0.6, nhalo=12, rms_cells=1.5)
+        return pos, rng.standard_normal(len(pos)).astype(np.float32), (16, 16, 16), (24.0, 24.0, 24.0)
+    if case == "ragged_edges":           # 1000 particles, prelude wraps, edge stencils
+        pos = _positions(1000, (20, 20, 20), (20.0, 20.0, 20.0), 4, np.float32)
+        return pos, rng.uniform(0.5, 1.5, len(pos)).astype(np.float32), (20, 20, 20), (20.0, 20.0, 20.0)
+    raise ValueError(case)
+
+
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("case", ["exact_lattice", "lattice", "lattice_nz34", "lattice_nz33", "mixed",
+                                  "ragged_edges"])
+def test_paint_methods_runs_and_windows(jl, method, case):
+    pos, mass, nm, box = _paint_case(case)
+    m = np.ones(len(pos), np.float32) if mass is None else mass
+    ref = cic.paint(cic.box_to_mesh(pos, box, nm), m, nm)
+    ref64 = cic.paint(cic.box_to_mesh(pos.astype(np.float64), box, nm), m.astype(np.float64), nm)
+    out = torch.empty(nm, dtype=torch.float32, device="cuda")
+    b = _box(box, np.float32)
+    mp = ct.c_void_p(None) if mass is None else _p(_cuda(mass))
+    jl.call("jld_ppaint_box_method_f32", _st(), _p(_cuda(pos)), len(pos), mp, ct.c_float(1.0),
+            *nm, b.ctypes.data_as(ct.c_void_p), method, _p(out))
+    err = np.abs(out.cpu().numpy() - ref).max()
+    assert err <= 2e-5 * np.abs(ref64).max(), (case, method, err)
+
+
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_paint3d_matches_oracle(jl, dt):
     nm, box = (16, 16, 16), (10.0, 10.0, 10.0)
