@@ -62,9 +62,10 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
 // Warps walk 32 consecutive particles at a time (all lanes stay in the loop
 // for the shuffles); lanes whose stencils share a z face merge it before
-// the atomics (zpair32_flags).  The 16 x 2 layout with y pairing as well
-// (pairing_flags) measured slower here: a scalar atomic costs less than
-// the extra shuffles and ballots.
+// the atomics (zpair32_flags).  Also measured and slower here: a 16 x 2
+// lane layout that pairs y faces as well (a scalar atomic costs less than
+// the extra shuffles and ballots), 8- and 16-byte vector atomics over the
+// z runs, and per-warp shared-memory windows for clumps.
 // Occupancy matters more than registers here (latency-bound loads and
 // atomics): six CTAs of 256 threads per SM in single precision.
 template <typename T, bool BOX>

@@ -201,22 +201,15 @@ __device__ __forceinline__ bool corner_ok(const Corners<T>& c, int bits) {
   return c.ok[0][bits & 1] && c.ok[1][(bits >> 1) & 1] && c.ok[2][(bits >> 2) & 1];
 }
 
-// Pairing of neighbouring particles for scatters.  A warp takes 16
-// consecutive particles of two consecutive "rows" of rl particles (lanes
-// 0-15: p .. p+15, lanes 16-31: the same columns one row later), rl being
-// a hint for the row length of particles stored in lattice order (the mesh
-// z extent).  A particle whose stencil does not wrap on any axis gets the
-// key "offset of its lower corner", others kNoPair.
-//   z pairing: if lane l (l mod 16 > 0) has key K and lane l-1 key K-1, lane
-//   l-1's upper-z face (corners 001 101 011 111) is lane l's lower-z face
-//   (000 100 010 110): lane l adds those four values to its own and lane
-//   l-1 skips their atomics.
-//   y pairing: if lane l >= 16 has key K and lane l-16 key K - sy, the
-//   upper-y corners of lane l-16 still held after z pairing move to lane l:
-//   010 110 always, 011 111 when neither lane gave its upper-z face away.
-// Every value is added by exactly one lane, so the result never depends on
-// the hint or on the pairing rate; particles in lattice order pair most of
-// the time, which removes most of their atomics.
+// Pairing of neighbouring particles for scatters.  A warp takes 32
+// consecutive particles.  A particle whose stencil does not wrap on any
+// axis gets the key "offset of its lower corner", others kNoPair.  If lane
+// l has key K and lane l-1 key K-1, lane l-1's upper-z face (corners 001
+// 101 011 111) is lane l's lower-z face (000 100 010 110): lane l adds those
+// four values to its own and lane l-1 skips their atomics.  Every value is
+// added by exactly one lane, so the result never depends on the pairing
+// rate; particles in lattice order (z fastest) pair most of the time, which
+// removes about half of their atomics.
 constexpr uint32_t kNoPair = 0xffffffffu;
 
 template <typename T>
@@ -227,34 +220,10 @@ __device__ __forceinline__ uint32_t pair_key(const Corners<T>& c, const Grid3& g
 }
 
 struct Pairing {
-  bool tz, gz;    // takes / gives the upper-z face (z pairing)
-  bool ty, gy;    // takes / gives corners 010 110 (y pairing)
-  bool thz, ghz;  // takes / gives corners 011 111 (y pairing of held upper-z corners)
+  bool tz, gz;    // takes / gives the upper-z face
 };
 
-// Warp-collective (all 32 lanes, the 16 x 2 layout above).
-__device__ __forceinline__ Pairing pairing_flags(uint32_t key, uint32_t sy) {
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31, g = lane & 15;
-  const uint32_t kz = __shfl_up_sync(full, key, 1);
-  const uint32_t ky = __shfl_up_sync(full, key, 16);
-  Pairing p;
-  p.tz = g > 0 && key != kNoPair && kz != kNoPair && key == kz + 1u;
-  const unsigned bz = __ballot_sync(full, p.tz);
-  p.gz = g < 15 && ((bz >> (lane + 1)) & 1u);
-  p.ty = lane >= 16 && key != kNoPair && ky != kNoPair && key == ky + sy;
-  const unsigned bgz = __ballot_sync(full, p.gz);
-  const bool gz_sender = lane >= 16 && ((bgz >> (lane - 16)) & 1u);
-  p.thz = p.ty && !p.gz && !gz_sender;
-  const unsigned by = __ballot_sync(full, p.ty), bh = __ballot_sync(full, p.thz);
-  p.gy = lane < 16 && ((by >> (lane + 16)) & 1u);
-  p.ghz = lane < 16 && ((bh >> (lane + 16)) & 1u);
-  return p;
-}
-
-// z pairing only, for 32 consecutive particles per warp (lane l absorbs
-// lane l-1's upper-z face): fewer shuffles and ballots than the 16 x 2
-// layout, for scatters whose atomics are cheap next to those instructions.
+// Warp-collective (all 32 lanes): lane l absorbs lane l-1's upper-z face.
 __device__ __forceinline__ Pairing zpair32_flags(uint32_t key) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -263,7 +232,6 @@ __device__ __forceinline__ Pairing zpair32_flags(uint32_t key) {
   p.tz = lane > 0 && key != kNoPair && kz != kNoPair && key == kz + 1u;
   const unsigned bz = __ballot_sync(full, p.tz);
   p.gz = lane < 31 && ((bz >> (lane + 1)) & 1u);
-  p.ty = p.gy = p.thz = p.ghz = false;
   return p;
 }
 
@@ -274,42 +242,7 @@ __device__ __forceinline__ constexpr int zpair_lo(int j) { return j == 0 ? 0 : j
 
 // Whether corner k is still added by this lane after pairing.
 __device__ __forceinline__ bool pair_keeps(const Pairing& p, int k) {
-  if (k == 0 || k == 1) return true;
-  if (k == 2 || k == 4) return !p.gy;
-  if (k == 3 || k == 5) return !p.gz;
-  return !p.gz && !p.ghz;  // k == 6, 7
+  return (k == 0 || k == 1 || k == 2 || k == 4) ? true : !p.gz;
 }
-
-// Warp walk over the tasks of the 16 x 2 layout (grid-stride over tasks;
-// the task -> (row pair, 16-column chunk) split is advanced incrementally,
-// without a 64-bit division per iteration).
-struct PairWalk {
-  int64_t n, rl, cpr, ntask, nw, spr, sc;  // sizes; per-iteration stride in (row pair, chunk)
-  int64_t task, pr, c;                     // current task and its (row pair, chunk)
-  __device__ __forceinline__ PairWalk(int64_t n_, int rl_) : n(n_), rl(rl_) {
-    cpr = (rl + 15) / 16;
-    ntask = ((n + rl - 1) / rl + 1) / 2 * cpr;
-    nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    spr = nw / cpr;
-    sc = nw - spr * cpr;
-    task = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    pr = task / cpr;
-    c = task - pr * cpr;
-  }
-  __device__ __forceinline__ bool more() const { return task < ntask; }
-  __device__ __forceinline__ void next() {
-    task += nw;
-    pr += spr;
-    c += sc;
-    if (c >= cpr) { c -= cpr; ++pr; }
-  }
-  // particle index of this lane in the current task, or -1
-  __device__ __forceinline__ int64_t particle() const {
-    const int lane = threadIdx.x & 31;
-    const int64_t col = c * 16 + (lane & 15);
-    const int64_t p = (2 * pr + (lane >> 4)) * rl + col;
-    return (col < rl && p < n) ? p : -1;
-  }
-};
 
 }  // namespace jld

@@ -403,11 +403,17 @@ static int ldl_step(const StepArgs& a) {
 
   // ---------------- final map, loss and its cotangent
   float* rho_f = rho + (size_t)L.C * a.nstep;
-  loss_kernel<<<cgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
-                                        a.L1, npix, rb, part);
-  JLD_LAUNCH_CHECK("loss_kernel");
-  launch_finish(st, part, (int)cgrid, 4, 1, a.out, 0, npix);
-  if (a.kind == 0) launch_finish(st, part + 1, (int)cgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
+  {
+    auto al16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+    const int vec4 = L.C % 4 == 0 && al16(rho_f) && al16(a.target) && al16(rb) && (!a.mask || al16(a.mask));
+    const unsigned lgrid = (unsigned)std::min<int64_t>(
+        kMaxCellBlocks, resident_grid(loss_kernel, vec4 ? L.C / 4 : L.C, cblock));
+    loss_kernel<<<lgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
+                                          a.L1, npix, rb, part, vec4);
+    JLD_LAUNCH_CHECK("loss_kernel");
+    launch_finish(st, part, (int)lgrid, 4, 1, a.out, 0, npix);
+    if (a.kind == 0) launch_finish(st, part + 1, (int)lgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
+  }
   if (!fuse_adj) {
     gather_vjp_kernel<<<resident_grid(gather_vjp_kernel, a.N, pblock), pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
     JLD_LAUNCH_CHECK("gather_vjp_kernel");
