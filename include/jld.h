@@ -108,6 +108,14 @@ JLD_API int jld_ppaint_box_f64(jld_stream_t stream, const double* pos, int64_t n
                        int64_t nx, int64_t ny, int64_t nz, const double box[3],
                        double* out);
 
+/* Accumulating box-unit paint: jld_ppaint_box_f32 without clearing `out` */
+/* first, so that particles arriving in chunks (snapshot ingestion,       */
+/* JERALD/snaputils.py:385-387 over a whole snapshot) add into one map.   */
+JLD_API int jld_ppaint_box_acc_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                           const float* mass, float mass_scalar,
+                           int32_t nx, int32_t ny, int32_t nz,
+                           const float box[3], float* out);
+
 /* Paint variants of the same box-unit paint (no reference counterpart;  */
 /* same contract and results within float rounding):                    */
 /*   method 0 = plain atomics, 1 = warp-aggregated atomics.             */
@@ -299,6 +307,25 @@ JLD_API int jld_ldl_order_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz
 JLD_API int jld_ldl_positions_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,
                                   int64_t nparts, int32_t nstep, int32_t layer,
                                   const float** out);
+
+/* ------------------------------------------------------------------ */
+/* Snapshot-map ingestion: the per-particle part of makemap              */
+/* (JERALD/snaputils.py:253-406) for one chunk of snapshot particles.    */
+/* pos_out = (pos / unit) % box (snaputils.py:379-380: float32 division, */
+/* then the periodic wrap in float64, rounded to float32); for kind > 0, */
+/* weights = the map kind's weight (snaputils.py:360-376) in float64,    */
+/* rounded to float32.  Kinds: 0 dm (no weights), 1 Mstar, 2 ne, 3 nT,   */
+/* 4 nHI, 5 neVz, 6 MstarVz, 7 XHI.  Fields a kind does not use may be    */
+/* NULL; particle p's vz is vz[vz_stride * p] (vz_stride 3 and vz = the  */
+/* Velocities array + 2 for (N, 3) velocities).                          */
+/* c1 = 4.0475e-7 h^2 / a^3 XH / prod(box) * prod(Nmesh), c2 = 323.06014 */
+/* (snaputils.py:351-355), sqrt_a = a^0.5.                               */
+JLD_API int jld_snap_prep_f32(jld_stream_t stream, const float* pos, int64_t nparts, float unit,
+                      const double box[3], int32_t kind, const float* masses,
+                      const float* electron_abundance, const float* internal_energy,
+                      const float* neutral_h_abundance, const float* vz, int64_t vz_stride,
+                      double c1, double c2, double XH, double sqrt_a,
+                      float* pos_out, float* weights);
 
 #ifdef __cplusplus
 }

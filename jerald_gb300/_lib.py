@@ -26,6 +26,10 @@ _SIGS = {
     "jld_ppaint_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _i32, _i32, _i32, _c_void_p],
     "jld_ppaint_f64": [_c_void_p, _c_void_p, _i64, _c_void_p, _i64, _i64, _i64, _c_void_p],
     "jld_ppaint_box_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _f32, _i32, _i32, _i32, _c_void_p, _c_void_p],
+    "jld_ppaint_box_acc_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _f32, _i32, _i32, _i32, _c_void_p,
+                               _c_void_p],
+    "jld_snap_prep_f32": [_c_void_p, _c_void_p, _i64, _f32, _c_void_p, _i32, _c_void_p, _c_void_p, _c_void_p,
+                          _c_void_p, _c_void_p, _i64, _f64, _f64, _f64, _f64, _c_void_p, _c_void_p],
     "jld_ppaint_box_f64": [_c_void_p, _c_void_p, _i64, _c_void_p, _f64, _i64, _i64, _i64, _c_void_p, _c_void_p],
     "jld_ppaint_box_method_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _f32, _i32, _i32, _i32, _c_void_p, _i32,
                                   _c_void_p],

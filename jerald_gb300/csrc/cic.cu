@@ -311,13 +311,13 @@ static PosSrc<T> make_src(const T* pos, const T* box, int64_t nx, int64_t ny,
 template <typename T>
 static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* mass,
                       T mscalar, int64_t nx, int64_t ny, int64_t nz, const T* box,
-                      int method, T* out, const char* who, bool fast = false) {
+                      int method, T* out, const char* who, bool fast = false, bool clear = true) {
   int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
   if (s) return s;
   if (box && !(box[0] > 0 && box[1] > 0 && box[2] > 0))
     return set_error(JLD_ERR_ARG, "%s: box sizes must be positive", who);
   Grid3 g = make_grid(nx, ny, nz);
-  JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(T) * g.cells(), st));
+  if (clear) JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(T) * g.cells(), st));
   if (nparts == 0) return JLD_OK;
   PosSrc<T> src = make_src<T>(pos, box, nx, ny, nz);
   src.fast = fast ? 1 : 0;
@@ -444,6 +444,14 @@ int jld_ppaint_box_f32(jld_stream_t s, const float* pos, int64_t n, const float*
   clear_error();
   if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint_box_f32: box is NULL");
   return paint_impl<float>(ST(s), pos, n, mass, ms, nx, ny, nz, box, 0, out, "jld_ppaint_box_f32");
+}
+int jld_ppaint_box_acc_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass,
+                           float ms, int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                           float* out) {
+  clear_error();
+  if (!box) return set_error(JLD_ERR_ARG, "jld_ppaint_box_acc_f32: box is NULL");
+  return paint_impl<float>(ST(s), pos, n, mass, ms, nx, ny, nz, box, 0, out, "jld_ppaint_box_acc_f32",
+                           false, false);
 }
 int jld_ppaint_box_f64(jld_stream_t s, const double* pos, int64_t n, const double* mass,
                        double ms, int64_t nx, int64_t ny, int64_t nz, const double box[3],

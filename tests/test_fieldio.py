@@ -1,0 +1,94 @@
+"""Bigfile-layout mesh files (maputils.savefield / loadfield restated without
+the bigfile module) and the host logic of the snapshot ingestion: CPU only."""
+import types
+
+import numpy as np
+import pytest
+
+from jerald_gb300 import fieldio
+
+
+def _pm(nm, box):
+    return types.SimpleNamespace(Nmesh=np.asarray(nm, dtype=np.int64), BoxSize=np.asarray(box, dtype=np.float64),
+                                 fftss=(0, nm[0]))
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("nfile", [1, 3])
+def test_field_roundtrip(tmp_path, dt, nfile):
+    nm, box = (6, 5, 4), (10.0, 12.5, 8.0)
+    data = np.random.default_rng(0).standard_normal(nm).astype(dt)
+    fieldio.savefield(data, tmp_path / "m", _pm(nm, box), nfile=nfile)
+    out, Nmesh, BoxSize = fieldio.loadfield(tmp_path / "m", verify=True)
+    assert out.dtype == dt and out.shape == nm
+    np.testing.assert_array_equal(out, data)
+    np.testing.assert_array_equal(Nmesh, nm)
+    np.testing.assert_array_equal(BoxSize, box)
+    loc, _, _ = fieldio.loadfield(tmp_path / "m", local=True, pm=_pm(nm, box))
+    np.testing.assert_array_equal(loc, data)
+
+
+def test_block_layout_and_attributes(tmp_path):
+    data = np.arange(10, dtype=np.float32)
+    fieldio.savefield(data.reshape(1, 2, 5), tmp_path / "f", _pm((1, 2, 5), (3.0, 4.0, 5.0)), nfile=2)
+    d = tmp_path / "f" / "Field"
+    assert sorted(p.name for p in d.iterdir()) == ["000000", "000001", "attr-v2", "header"]
+    lines = (d / "header").read_text().splitlines()
+    assert lines[:3] == ["DTYPE: <f4", "NMEMB: 1", "NFILE: 2"]
+    ck, sv = fieldio.sysv_checksums(data[:5].tobytes())
+    assert lines[3] == f"000000: 5 : {ck} : {sv}"
+    attrs = fieldio.read_attrs(tmp_path / "f", "Field")
+    assert set(attrs) == {"ndarray.shape", "BoxSize", "Nmesh"}
+    assert attrs["Nmesh"].dtype == np.dtype("<i8") and list(attrs["Nmesh"]) == [1, 2, 5]
+    assert attrs["BoxSize"].dtype == np.dtype("<f8") and list(attrs["BoxSize"]) == [3.0, 4.0, 5.0]
+    first = (d / "attr-v2").read_text().splitlines()[0]
+    assert first.startswith("ndarray.shape <i8 3 0100000000000000") and "#HUMANE [ 1 2 5 ]" in first
+
+
+def test_sysv_checksum_known_values():
+    assert fieldio.sysv_checksums(b"abc") == (294, 294)
+    s, sv = fieldio.sysv_checksums(bytes([255]) * 1000)
+    assert s == 255000 and sv == ((255000 & 0xFFFF) + (255000 >> 16))
+
+
+def test_corruption_is_detected(tmp_path):
+    data = np.ones((2, 2, 2), dtype=np.float32)
+    fieldio.savefield(data, tmp_path / "c", _pm((2, 2, 2), (1.0, 1.0, 1.0)))
+    p = tmp_path / "c" / "Field" / "000000"
+    raw = bytearray(p.read_bytes())
+    raw[0] ^= 1
+    p.write_bytes(bytes(raw))
+    with pytest.raises(ValueError, match="checksum"):
+        fieldio.loadfield(tmp_path / "c", verify=True)
+    (tmp_path / "c" / "Field" / "header").write_text("DTYPE: <f4\nNMEMB: 1\nNFILE: 2\n000000: 8 : 0 : 0\n")
+    with pytest.raises(ValueError, match="incomplete"):
+        fieldio.loadfield(tmp_path / "c")
+
+
+def test_snapshot_host_logic(tmp_path):
+    from jerald_gb300 import snapmap
+    assert [snapmap.mapPartNum(k) for k in ("dm", "Mstar", "MstarVz", "ne", "nT", "nHI", "neVz", "XHI")] == \
+        [1, 4, 4, 0, 0, 0, 0, 0]
+    with pytest.raises(ValueError):
+        snapmap.mapPartNum("gas")
+    f, mdi = snapmap.map_fields("neVz")
+    assert f == ["Coordinates", "Masses", "ElectronAbundance", "Velocities"] and mdi == [None, None, None, 2]
+    assert snapmap.map_fields("nT")[0] == ["Coordinates", "ElectronAbundance", "InternalEnergy", "Masses"]
+    a, c1, c2 = snapmap.map_coefficients(2.0, [25.0] * 3, [64] * 3, h=0.7, XH=0.76)
+    assert a == 1 / 3 and c2 == 323.06014
+    assert c1 == 4.0475e-07 * 0.7 ** 2 / (1 / 3) ** 3 * 0.76 / 25.0 ** 3 * 64 ** 3
+    # snapshot path resolution (snaputils.fname)
+    (tmp_path / "snap_004.0.hdf5").write_bytes(b"")
+    (tmp_path / "snap_004.1.hdf5").write_bytes(b"")
+    base = str(tmp_path / "snap_004")
+    assert snapmap.fname(base) == base + ".0.hdf5"
+    assert snapmap.fname(base + ".1") == base + ".0.hdf5"
+    assert snapmap.fname(base + ".1.hdf5") == base + ".1.hdf5"
+    with pytest.raises(FileNotFoundError):
+        snapmap.fname(str(tmp_path / "nothing"))
+    snap = snapmap.ArraySnapshot(0.5, {0: {"Coordinates": np.zeros((10, 3), np.float32),
+                                           "Velocities": np.arange(30, dtype=np.float32).reshape(10, 3)}})
+    assert list(snap.nall) == [10, 0, 0, 0, 0, 0]
+    ch = list(snap.chunks(0, ["Coordinates", "Velocities"], [None, 2], 4))
+    assert [len(c["Coordinates"]) for c in ch] == [4, 4, 2]
+    np.testing.assert_array_equal(np.concatenate([c["Velocities"] for c in ch]), np.arange(2, 30, 3))
