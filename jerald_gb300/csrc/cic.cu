@@ -66,10 +66,14 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 // lane layout that pairs y faces as well (a scalar atomic costs less than
 // the extra shuffles and ballots), 8- and 16-byte vector atomics over the
 // z runs, and per-warp shared-memory windows for clumps.
-// Occupancy matters more than registers here (latency-bound loads and
-// atomics): six CTAs of 256 threads per SM in single precision.
+// Six CTAs of 256 threads per SM in single precision (40 registers): on the
+// 512^3 clustered step five and six tie, seven and eight (32 registers, full
+// occupancy) are 0.7 ms slower, more warps queueing on the same atomics.
+#ifndef JLD_PAINT_MIN_CTAS
+#define JLD_PAINT_MIN_CTAS 6
+#endif
 template <typename T, bool BOX>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 3)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? JLD_PAINT_MIN_CTAS : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;

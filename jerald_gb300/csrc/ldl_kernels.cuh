@@ -425,9 +425,11 @@ __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int
 }
 
 // X' = X + readout of the float4 force mesh (three channels, the reference's
-// per-channel summation order).
+// per-channel summation order).  Five CTAs per SM (48 registers): on the
+// 512^3 clustered step 29.9 ms against 30.1 at six (40 registers) and 31.8
+// at seven (32 registers, spills).
 #ifndef JLD_UPD_MIN_CTAS
-#define JLD_UPD_MIN_CTAS 6
+#define JLD_UPD_MIN_CTAS 5
 #endif
 __global__ void __launch_bounds__(256, JLD_UPD_MIN_CTAS)
 update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
