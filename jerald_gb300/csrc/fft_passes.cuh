@@ -51,7 +51,7 @@ template <typename T, int SCHED>
 __global__ void __launch_bounds__(512)
 line_pass_kernel(LinePlan<T> pl, LineJob<T> j0, LineJob<T> j1, int cols, int cshift, int sgn) {
   using C = cplx_t<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colin[64], colout[64];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -113,7 +113,7 @@ rfft_z_kernel(LinePlan<T> pl, const cplx_t<T>* __restrict__ twr, const T* __rest
               Src src, cplx_t<T>* __restrict__ main, cplx_t<T>* __restrict__ nyq,
               int64_t rows, int cols, int cshift) {
   using C = cplx_t<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int h = pl.n, ld = cols + 1;
@@ -172,7 +172,7 @@ irfft_z_kernel(LinePlan<T> pl, const cplx_t<T>* __restrict__ twr,
                const cplx_t<T>* __restrict__ main, const cplx_t<T>* __restrict__ nyq,
                T* __restrict__ out, Dst dst, int64_t rows, int cols, int cshift) {
   using C = cplx_t<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int h = pl.n, ld = cols + 1;

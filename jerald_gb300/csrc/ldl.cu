@@ -620,7 +620,7 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   if (options & ~kOptAll) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
   if ((options & kOptBinned) && nparts > INT32_MAX)
     return set_error(JLD_ERR_UNSUPPORTED, "%s: binning needs fewer than 2^31 particles", who);
-  const int paint_method = options & 1;
+  const int paint_method = (options & kOptWarpPaint) ? 1 : 0;
   if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
   size_t need = ldl_layout(nx, ny, nz, nparts, nstep, options).total;
   if (!ws || ws_bytes < need)

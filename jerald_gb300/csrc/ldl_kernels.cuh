@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(512)
 xfilt_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict__ params,
              int kind, float scale, const float2* __restrict__ A, float2* __restrict__ S,
              float2* __restrict__ T0, float2* __restrict__ T1) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(512)
 yinv3_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float2* __restrict__ T0,
              const float2* __restrict__ T1, float2* __restrict__ Gx, float2* __restrict__ Gy,
              float2* __restrict__ Gz) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(512)
 zinv3_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2* __restrict__ Gx,
              const float2* __restrict__ Gy, const float2* __restrict__ Gz, int64_t nyq_off,
              float4* __restrict__ g4, int64_t rows, int cols, int cshift) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int h = pl.n, ld = cols + 1;
   float2* sm[3];
@@ -713,7 +713,7 @@ zinv_adj_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float2
                 int64_t nyq_off, const float* __restrict__ rho_paint, const float* __restrict__ params,
                 float fact, float* __restrict__ rb, double* __restrict__ partials, int64_t rows,
                 int cols, int cshift) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   float2* sm = reinterpret_cast<float2*>(smraw);
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int h = pl.n, ld = cols + 1;
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(512)
 zfwd3_kernel(LinePlan<float> pl, const float2* __restrict__ twr, const float* __restrict__ cz,
              const float4* __restrict__ gb4, float2* __restrict__ Ax, float2* __restrict__ Ay,
              float2* __restrict__ Az, int64_t nyq_off, int64_t rows, int cols, int cshift) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int h = pl.n, ld = cols + 1;
   float2* sm[3];
@@ -813,7 +813,7 @@ __global__ void __launch_bounds__(512)
 yfwd_comb_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, float2* __restrict__ Ax,
                  const float2* __restrict__ Ay, const float2* __restrict__ Az,
                  float2* __restrict__ D) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(512)
 xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict__ params, int kind,
             int mode, float scale, const float2* __restrict__ Bx, const float2* __restrict__ D,
             const float2* __restrict__ S, float2* __restrict__ Vout, double* __restrict__ partials) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
