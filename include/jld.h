@@ -294,6 +294,25 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
                              int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
                              int32_t options, const float* params, const float* target,
                              const float* mask, void* ws, size_t ws_bytes, double* out);
+/* The rest of model.py's loss for the fused step (jld_ldl_step_ext_f32): */
+/* the smoothing of the residual by |k|^-n + 1 (model.py:376-381), the map */
+/* exponent and second field (model.py:357-361) and the validation loss   */
+/* (model.py:416-465).  Mask, field2 and maskvalid are (Nx, Ny, Nz) float  */
+/* meshes on the device.                                                  */
+typedef struct jld_ldl_loss_ext {
+  float n;                /* smoothing exponent; 0 = no smoothing          */
+  float index;            /* F ** index; 1 = none                           */
+  const float* field2;    /* F * field2, or NULL                            */
+  const float* maskvalid; /* validation mask, or NULL (validation loss 0)   */
+} jld_ldl_loss_ext;
+/* jld_ldl_step_f32 with the loss options above; out holds one more value */
+/* after the gradient: the validation loss (model.py:lossv).              */
+JLD_API int jld_ldl_step_ext_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                                 int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                                 int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
+                                 int32_t options, const float* params, const float* target,
+                                 const float* mask, const jld_ldl_loss_ext* ext, void* ws,
+                                 size_t ws_bytes, double* out);
 /* Device pointer to the step's error word in `ws` (0 = fine; nonzero = a  */
 /* pipelined pass gave up waiting for a tile copy and stopped early).      */
 JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,

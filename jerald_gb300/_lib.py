@@ -63,6 +63,8 @@ _SIGS = {
     "jld_ldl_prepare_f32": [_i32, _i32, _i32, _c_void_p],
     "jld_ldl_step_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32, _i32,
                          _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
+    "jld_ldl_step_ext_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32,
+                             _i32, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
     "jld_ldl_positions_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _i32, _c_void_p],
     "jld_ldl_error_word_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
     "jld_ldl_order_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],

@@ -91,8 +91,12 @@ struct StepArgs {
   int options;           // option bits (layout)
   const float* params;   // device: 5*nstep (+3 for kind 0)
   const float* target; const float* mask;
+  float n, index;        // loss smoothing exponent (0: none), map exponent (1: none)
+  const float* field2;   // map factor or nullptr
+  const float* maskvalid;  // validation mask or nullptr
+  bool lossv_slot;       // out holds the validation loss after the gradient
   char* ws;
-  double* out;           // device: [loss, grads...]
+  double* out;           // device: [loss, grads... (, validation loss)]
 };
 
 struct SpecGeom {
@@ -216,15 +220,19 @@ static int ldl_step(const StepArgs& a) {
   if (gx.tiles * 4 > L.part_doubles || (int64_t)zgrid > L.part_doubles)
     return set_error(JLD_ERR_UNSUPPORTED, "mesh too large for the reduction buffer");
 
-  // 1 / Npixel in FP64 (model.py:386-390)
-  if (a.mask) {
-    mask_count_kernel<<<cgrid, cblock, 0, st>>>(a.mask, L.C, part);
-    JLD_LAUNCH_CHECK("mask_count_kernel");
-    finish_kernel<<<1, 256, 0, st>>>(part, (int)cgrid, 1, 1, npix, 0, nullptr, 1);
-    JLD_LAUNCH_CHECK("finish_kernel");
-  } else {
-    set_scalar_kernel<<<1, 1, 0, st>>>(npix, 1.0 / (double)L.C);
-    JLD_LAUNCH_CHECK("set_scalar_kernel");
+  // 1 / Npixel in FP64 (model.py:386-390), then 1 / Npixel of the
+  // validation mask (model.py:458-463)
+  for (int v = 0; v < 2; ++v) {
+    const float* m = v ? a.maskvalid : a.mask;
+    if (m) {
+      mask_count_kernel<<<cgrid, cblock, 0, st>>>(m, L.C, part);
+      JLD_LAUNCH_CHECK("mask_count_kernel");
+      finish_kernel<<<1, 256, 0, st>>>(part, (int)cgrid, 1, 1, npix, v, nullptr, 1);
+      JLD_LAUNCH_CHECK("finish_kernel");
+    } else if (v == 0) {
+      set_scalar_kernel<<<1, 1, 0, st>>>(npix, 1.0 / (double)L.C);
+      JLD_LAUNCH_CHECK("set_scalar_kernel");
+    }
   }
 
   // ---------------- pipelined (TMA-staged) strided passes, when the mesh qualifies
@@ -404,15 +412,51 @@ static int ldl_step(const StepArgs& a) {
   // ---------------- final map, loss and its cotangent
   float* rho_f = rho + (size_t)L.C * a.nstep;
   {
-    auto al16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
-    const int vec4 = L.C % 4 == 0 && al16(rho_f) && al16(a.target) && al16(rb) && (!a.mask || al16(a.mask));
-    const unsigned lgrid = (unsigned)std::min<int64_t>(
-        kMaxCellBlocks, resident_grid(loss_kernel, vec4 ? L.C / 4 : L.C, cblock));
-    loss_kernel<<<lgrid, cblock, 0, st>>>(rho_f, a.target, a.mask, L.C, fact, a.params + 5 * a.nstep, a.kind,
-                                          a.L1, npix, rb, part, vec4);
-    JLD_LAUNCH_CHECK("loss_kernel");
-    launch_finish(st, part, (int)lgrid, 4, 1, a.out, 0, npix);
-    if (a.kind == 0) launch_finish(st, part + 1, (int)lgrid, 4, 3, a.out, 1 + 5 * a.nstep, nullptr);
+    const LossFields lf{rho_f, a.target, a.mask, a.field2, a.maskvalid};
+    const float* fprm = a.params + 5 * a.nstep;
+    const int nparam = 5 * a.nstep + (a.kind == 0 ? 3 : 0);
+    const int64_t max_blocks = std::min<int64_t>(kMaxCellBlocks, L.part_doubles / 5);
+    // validation loss: reduced only with a validation mask, else 0
+    double* lossv_out = a.lossv_slot ? a.out + 1 + nparam : nullptr;
+    if (lossv_out && !a.maskvalid) JLD_CUDA_TRY(cudaMemsetAsync(lossv_out, 0, sizeof(double), st));
+    if (a.n > 0.f) {
+      // diff -> c2r(r2c(diff) K) -> loss -> the same smoothing on its
+      // cotangent (a real, even Fourier multiplier is its own adjoint)
+      const size_t wbytes = al(sizeof(float2) * L.H);
+      auto smooth = [&](float* f) -> int {
+        int r = jld_pfft_c_f32((jld_stream_t)st, f, nx, ny, nz, W[0], W[1], wbytes);
+        if (r) return r;
+        smooth_spec_kernel<<<resident_grid(smooth_spec_kernel, L.H, cblock), cblock, 0, st>>>(
+            W[0], nx, ny, h + 1, kt, a.n, scale);
+        JLD_LAUNCH_CHECK("smooth_spec_kernel");
+        return jld_pifft_c_f32((jld_stream_t)st, W[0], nx, ny, nz, f, W[1], wbytes);
+      };
+      const unsigned g1 = (unsigned)std::min<int64_t>(max_blocks, resident_grid(smooth_map_kernel, L.C, cblock));
+      smooth_map_kernel<<<g1, cblock, 0, st>>>(lf, L.C, fact, fprm, a.kind, a.index, rb);
+      JLD_LAUNCH_CHECK("smooth_map_kernel");
+      if ((s = smooth(rb))) return s;
+      const unsigned g2 = (unsigned)std::min<int64_t>(max_blocks, resident_grid(smooth_loss_kernel, L.C, cblock));
+      smooth_loss_kernel<<<g2, cblock, 0, st>>>(lf, L.C, a.L1, npix, rb, part);
+      JLD_LAUNCH_CHECK("smooth_loss_kernel");
+      launch_finish(st, part, (int)g2, 2, 1, a.out, 0, npix);
+      if (lossv_out && a.maskvalid) launch_finish(st, part + 1, (int)g2, 2, 1, a.out, 1 + nparam, npix + 1);
+      if ((s = smooth(rb))) return s;
+      const unsigned g3 = (unsigned)std::min<int64_t>(max_blocks, resident_grid(smooth_adj_kernel, L.C, cblock));
+      smooth_adj_kernel<<<g3, cblock, 0, st>>>(lf, L.C, fact, fprm, a.kind, a.index, rb, part);
+      JLD_LAUNCH_CHECK("smooth_adj_kernel");
+      if (a.kind == 0) launch_finish(st, part, (int)g3, 3, 3, a.out, 1 + 5 * a.nstep, nullptr);
+    } else {
+      auto al16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+      const int vec4 = L.C % 4 == 0 && al16(rho_f) && al16(a.target) && al16(rb) && (!a.mask || al16(a.mask)) &&
+                       (!a.field2 || al16(a.field2)) && (!a.maskvalid || al16(a.maskvalid));
+      const unsigned lgrid = (unsigned)std::min<int64_t>(
+          max_blocks, resident_grid(loss_kernel, vec4 ? L.C / 4 : L.C, cblock));
+      loss_kernel<<<lgrid, cblock, 0, st>>>(lf, L.C, fact, fprm, a.kind, a.L1, a.index, npix, rb, part, vec4);
+      JLD_LAUNCH_CHECK("loss_kernel");
+      launch_finish(st, part, (int)lgrid, 5, 1, a.out, 0, npix);
+      if (a.kind == 0) launch_finish(st, part + 1, (int)lgrid, 5, 3, a.out, 1 + 5 * a.nstep, nullptr);
+      if (lossv_out && a.maskvalid) launch_finish(st, part + 4, (int)lgrid, 5, 1, a.out, 1 + nparam, npix + 1);
+    }
   }
   if (!fuse_adj) {
     gather_vjp_kernel<<<resident_grid(gather_vjp_kernel, a.N, pblock), pblock, 0, st>>>(Xl(a.nstep), a.N, bg, g, rb, Xb, 0);
@@ -604,13 +648,10 @@ JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float 
   return get_ktables(nx, ny, nz, box, true, &kt);
 }
 
-JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
-                             int32_t nz, const float box[3], int32_t nstep, int32_t kind, int32_t L1,
-                             int32_t grad_mode, int32_t options, const float* params,
-                             const float* target, const float* mask, void* ws, size_t ws_bytes,
-                             double* out) {
-  clear_error();
-  const char* who = "jld_ldl_step_f32";
+static int step_entry(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny, int32_t nz,
+                      const float box[3], int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
+                      int32_t options, const float* params, const float* target, const float* mask,
+                      const jld_ldl_loss_ext* ext, void* ws, size_t ws_bytes, double* out, const char* who) {
   int s = check_step_args(nx, ny, nz, nparts, nstep, box, who);
   if (s) return s;
   if (kind != 0 && kind != 1) return set_error(JLD_ERR_ARG, "%s: kind must be 0 (sm) or 1 (dm)", who);
@@ -639,8 +680,37 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
   a.binned = (options & kOptBinned) != 0;
   a.options = options;
   a.params = params; a.target = target; a.mask = mask;
+  a.n = ext ? ext->n : 0.f;
+  a.index = ext ? ext->index : 1.f;
+  a.field2 = ext ? ext->field2 : nullptr;
+  a.maskvalid = ext ? ext->maskvalid : nullptr;
+  a.lossv_slot = ext != nullptr;
+  if (!(a.n >= 0.f) || !std::isfinite(a.index))
+    return set_error(JLD_ERR_ARG, "%s: n must be >= 0 and index finite", who);
   a.ws = (char*)ws; a.out = out;
   return ldl_step(a);
+}
+
+JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
+                             int32_t nz, const float box[3], int32_t nstep, int32_t kind, int32_t L1,
+                             int32_t grad_mode, int32_t options, const float* params,
+                             const float* target, const float* mask, void* ws, size_t ws_bytes,
+                             double* out) {
+  clear_error();
+  return step_entry(stream, pos, nparts, nx, ny, nz, box, nstep, kind, L1, grad_mode, options, params, target,
+                    mask, nullptr, ws, ws_bytes, out, "jld_ldl_step_f32");
+}
+
+JLD_API int jld_ldl_step_ext_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
+                                 int32_t nz, const float box[3], int32_t nstep, int32_t kind, int32_t L1,
+                                 int32_t grad_mode, int32_t options, const float* params,
+                                 const float* target, const float* mask, const jld_ldl_loss_ext* ext, void* ws,
+                                 size_t ws_bytes, double* out) {
+  clear_error();
+  const char* who = "jld_ldl_step_ext_f32";
+  if (!ext) return set_error(JLD_ERR_ARG, "%s: ext is NULL", who);
+  return step_entry(stream, pos, nparts, nx, ny, nz, box, nstep, kind, L1, grad_mode, options, params, target,
+                    mask, ext, ws, ws_bytes, out, who);
 }
 
 JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,

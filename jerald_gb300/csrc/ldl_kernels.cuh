@@ -635,74 +635,192 @@ __device__ __forceinline__ void block_reduce_kahan(const KahanF (&k)[NV], double
   block_reduce_store<NV>(v, out, slot_stride);
 }
 
-// Final map, loss and its cotangent (model.py:311-403).  Partials per block:
-// [loss, d mu, d w, d b].  rb = fact * d loss / d rho.
+// Final map, loss and its cotangent (model.py:311-403, 351-403, 416-465).
+// F = ReLU(w (rho + 1e-8)^mu + b) (kind sm) or rho (kind dm); the loss map is
+// Fp = F^index * field2 (model.py:357-361); diff = Fp - target, smoothed by
+// c2r(r2c(diff) K) with K = |k|^-n + 1 when n > 0 (model.py:376-381, no c2f);
+// loss = sum (mask |diff|)^p / Npixel, the validation loss the same with
+// maskvalid (model.py:454-465).  rb = fact * d loss / d rho.
 struct LossArgs {
-  float mu, w, b, fact, inpx;
+  float mu, w, b, fact, inpx, index;
   int kind, L1;
 };
 
-__device__ __forceinline__ float loss_cell(const LossArgs& la, float rho_paint, float t, float m,
-                                           KahanF (&acc)[4]) {
+struct MapCell {
+  float F, u, pw, base, lnb;
+};
+
+__device__ __forceinline__ MapCell map_cell(const LossArgs& la, float rho_paint) {
+  MapCell c;
   const float rho = __fmul_rn(rho_paint, la.fact);
-  float F, base = 0.f, pw = 0.f, u = 0.f, lnb = 0.f;
+  c.u = c.pw = c.base = c.lnb = 0.f;
   if (la.kind == 0) {
-    base = __fadd_rn(rho, 1e-8f);
-    pw = pow_pos(base, la.mu, &lnb);
-    u = __fadd_rn(__fmul_rn(la.w, pw), la.b);
-    F = u > 1e-12f ? u : 1e-12f;
+    c.base = __fadd_rn(rho, 1e-8f);
+    c.pw = pow_pos(c.base, la.mu, &c.lnb);
+    c.u = __fadd_rn(__fmul_rn(la.w, c.pw), la.b);
+    c.F = c.u > 1e-12f ? c.u : 1e-12f;
   } else {
-    F = rho;
+    c.F = rho;
   }
-  const float diff = F - t;
-  const float ad = fabsf(diff) * m;
-  acc[0].add(la.L1 ? ad : ad * ad);
-  const float sg = diff >= 0.f ? 1.f : -1.f;
-  const float ctF = (la.L1 ? sg * m : 2.f * fabsf(diff) * m * m * sg) * la.inpx;
+  return c;
+}
+
+// Fp = F^index * f2; *dFp = dFp/dF.
+__device__ __forceinline__ float map_ext(const LossArgs& la, float F, float f2, float* dFp) {
+  float Fp = F, d = 1.f;
+  if (la.index != 1.f) {
+    Fp = pow_pos(F, la.index);
+    d = la.index * pow_pos(F, la.index - 1.f);
+  }
+  *dFp = d * f2;
+  return Fp * f2;
+}
+
+// Adjoint of the map for ctF = dL/dF: (d mu, d w, d b) into acc3 (kind sm);
+// returns fact * dL/drho.
+__device__ __forceinline__ float map_adjoint(const LossArgs& la, const MapCell& c, float ctF, KahanF* acc3) {
   if (la.kind == 0) {
-    const float ctu = u > 1e-12f ? ctF : 0.f;
-    acc[1].add(ctu * la.w * pw * lnb);
-    acc[2].add(ctu * pw);
-    acc[3].add(ctu);
+    const float ctu = c.u > 1e-12f ? ctF : 0.f;
+    acc3[0].add(ctu * la.w * c.pw * c.lnb);
+    acc3[1].add(ctu * c.pw);
+    acc3[2].add(ctu);
     // base^(mu-1) = pw / base (base > 0)
-    return ctu * la.w * la.mu * (pw / base) * la.fact;
+    return ctu * la.w * la.mu * (c.pw / c.base) * la.fact;
   }
   return ctF * la.fact;
 }
 
-// Cells in float4 groups (vec4: every array 16-byte aligned, C a multiple
-// of 4), the rest one by one.
-__global__ void __launch_bounds__(256)
-loss_kernel(const float* __restrict__ rho_paint, const float* __restrict__ target,
-            const float* __restrict__ mask, int64_t C, float fact, const float* __restrict__ fparams,
-            int kind, int L1, const double* __restrict__ inv_npix, float* __restrict__ rb,
-            double* __restrict__ partials, int vec4) {
+// Loss and validation-loss terms of one cell's residual; returns dL/d diff.
+__device__ __forceinline__ float diff_terms(const LossArgs& la, float diff, float m, float mv, KahanF& lacc,
+                                            KahanF& vacc) {
+  const float ad = fabsf(diff) * m;
+  lacc.add(la.L1 ? ad : ad * ad);
+  const float av = fabsf(diff) * mv;
+  vacc.add(la.L1 ? av : av * av);
+  const float sg = diff >= 0.f ? 1.f : -1.f;
+  return (la.L1 ? sg * m : 2.f * fabsf(diff) * m * m * sg) * la.inpx;
+}
+
+__device__ __forceinline__ LossArgs loss_args(const float* fparams, int kind, int L1, float fact, float index,
+                                              const double* inv_npix) {
   LossArgs la;
   la.mu = kind == 0 ? __ldg(fparams + 0) : 0.f;
   la.w = kind == 0 ? __ldg(fparams + 1) : 0.f;
   la.b = kind == 0 ? __ldg(fparams + 2) : 0.f;
   la.fact = fact;
-  la.inpx = (float)(*inv_npix);
+  la.inpx = inv_npix ? (float)(*inv_npix) : 0.f;
+  la.index = index;
   la.kind = kind;
   la.L1 = L1;
-  KahanF acc[4];
+  return la;
+}
+
+// The per-cell inputs of the loss (mask, field2, validation mask optional).
+struct LossFields {
+  const float* rho;
+  const float* target;
+  const float* mask;
+  const float* field2;
+  const float* maskvalid;
+};
+
+__device__ __forceinline__ float4 ld4_or(const float* p, int64_t e, float v) {
+  return p ? __ldg(reinterpret_cast<const float4*>(p) + e) : make_float4(v, v, v, v);
+}
+__device__ __forceinline__ float ld_or(const float* p, int64_t e, float v) { return p ? __ldg(p + e) : v; }
+__device__ __forceinline__ float f4c(const float4& v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+
+// Unsmoothed loss in one pass.  Partials per block: [loss, d mu, d w, d b,
+// validation loss].  Cells in float4 groups (vec4: every array 16-byte
+// aligned, C a multiple of 4), the rest one by one.
+__global__ void __launch_bounds__(256)
+loss_kernel(LossFields lf, int64_t C, float fact, const float* __restrict__ fparams, int kind, int L1,
+            float index, const double* __restrict__ inv_npix, float* __restrict__ rb,
+            double* __restrict__ partials, int vec4) {
+  const LossArgs la = loss_args(fparams, kind, L1, fact, index, inv_npix);
+  KahanF acc[5];
+  auto cell = [&](float r, float t, float m, float f2, float mv) {
+    const MapCell c = map_cell(la, r);
+    float dFp;
+    const float Fp = map_ext(la, c.F, f2, &dFp);
+    const float ct = diff_terms(la, Fp - t, m, mv, acc[0], acc[4]);
+    return map_adjoint(la, c, ct * dFp, acc + 1);
+  };
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nth = (int64_t)gridDim.x * blockDim.x;
   const int64_t c4 = vec4 ? C / 4 : 0;
   for (int64_t e = tid; e < c4; e += nth) {
-    const float4 r = __ldg(reinterpret_cast<const float4*>(rho_paint) + e);
-    const float4 t = __ldg(reinterpret_cast<const float4*>(target) + e);
-    const float4 m = mask ? __ldg(reinterpret_cast<const float4*>(mask) + e) : make_float4(1.f, 1.f, 1.f, 1.f);
-    float4 o;
-    o.x = loss_cell(la, r.x, t.x, m.x, acc);
-    o.y = loss_cell(la, r.y, t.y, m.y, acc);
-    o.z = loss_cell(la, r.z, t.z, m.z, acc);
-    o.w = loss_cell(la, r.w, t.w, m.w, acc);
-    reinterpret_cast<float4*>(rb)[e] = o;
+    const float4 r = __ldg(reinterpret_cast<const float4*>(lf.rho) + e);
+    const float4 t = __ldg(reinterpret_cast<const float4*>(lf.target) + e);
+    const float4 m = ld4_or(lf.mask, e, 1.f), f2 = ld4_or(lf.field2, e, 1.f), mv = ld4_or(lf.maskvalid, e, 0.f);
+    float o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = cell(f4c(r, q), f4c(t, q), f4c(m, q), f4c(f2, q), f4c(mv, q));
+    reinterpret_cast<float4*>(rb)[e] = make_float4(o[0], o[1], o[2], o[3]);
   }
   for (int64_t e = 4 * c4 + tid; e < C; e += nth)
-    rb[e] = loss_cell(la, __ldg(rho_paint + e), __ldg(target + e), mask ? __ldg(mask + e) : 1.f, acc);
-  block_reduce_kahan<4>(acc, partials, 4);
+    rb[e] = cell(__ldg(lf.rho + e), __ldg(lf.target + e), ld_or(lf.mask, e, 1.f), ld_or(lf.field2, e, 1.f),
+                 ld_or(lf.maskvalid, e, 0.f));
+  block_reduce_kahan<5>(acc, partials, 5);
+}
+
+// Smoothed loss, pass 1: rb = Fp - target.
+__global__ void __launch_bounds__(256)
+smooth_map_kernel(LossFields lf, int64_t C, float fact, const float* __restrict__ fparams, int kind,
+                  float index, float* __restrict__ rb) {
+  const LossArgs la = loss_args(fparams, kind, 1, fact, index, nullptr);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < C; e += (int64_t)gridDim.x * blockDim.x) {
+    const MapCell c = map_cell(la, __ldg(lf.rho + e));
+    float dFp;
+    rb[e] = map_ext(la, c.F, ld_or(lf.field2, e, 1.f), &dFp) - __ldg(lf.target + e);
+  }
+}
+
+// Smoothed loss, pass 2, on rb = the smoothed residual: partials per block
+// [loss, validation loss]; rb = dL / d(smoothed residual).
+__global__ void __launch_bounds__(256)
+smooth_loss_kernel(LossFields lf, int64_t C, int L1, const double* __restrict__ inv_npix, float* __restrict__ rb,
+                   double* __restrict__ partials) {
+  LossArgs la = loss_args(nullptr, 1, L1, 1.f, 1.f, inv_npix);
+  KahanF acc[2];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < C; e += (int64_t)gridDim.x * blockDim.x)
+    rb[e] = diff_terms(la, rb[e], ld_or(lf.mask, e, 1.f), ld_or(lf.maskvalid, e, 0.f), acc[0], acc[1]);
+  block_reduce_kahan<2>(acc, partials, 2);
+}
+
+// Smoothed loss, pass 3, on rb = dL/dFp: partials per block [d mu, d w, d b];
+// rb = fact * dL/drho.
+__global__ void __launch_bounds__(256)
+smooth_adj_kernel(LossFields lf, int64_t C, float fact, const float* __restrict__ fparams, int kind, float index,
+                  float* __restrict__ rb, double* __restrict__ partials) {
+  const LossArgs la = loss_args(fparams, kind, 1, fact, index, nullptr);
+  KahanF acc[3];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < C; e += (int64_t)gridDim.x * blockDim.x) {
+    const MapCell c = map_cell(la, __ldg(lf.rho + e));
+    float dFp;
+    (void)map_ext(la, c.F, ld_or(lf.field2, e, 1.f), &dFp);
+    rb[e] = map_adjoint(la, c, rb[e] * dFp, acc);
+  }
+  block_reduce_kahan<3>(acc, partials, 3);
+}
+
+// Smoothing kernel on an interleaved (Nx, Ny, Nz/2+1) half spectrum:
+// spec *= (|k|^-n + 1) * scale with |k| = 0 read as 1e-8 (model.py:100-102,
+// so the reference's |k| == 0 branch never applies).
+__global__ void __launch_bounds__(256)
+smooth_spec_kernel(float2* __restrict__ spec, int nx, int ny, int hh, KTables kt, float n, float scale) {
+  const int64_t H = (int64_t)nx * ny * hh;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < H; e += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(e % hh);
+    const int64_t r = e / hh;
+    const int j = (int)(r % ny), i = (int)(r / ny);
+    const float kx = __ldg(kt.kx + i), ky = __ldg(kt.ky + j), kz = __ldg(kt.kz + l);
+    float k = sqrtf(kx * kx + ky * ky + kz * kz);
+    if (k == 0.f) k = 1e-8f;
+    const float K = __fadd_rn(exp2f(-n * log2f(k)), 1.f) * scale;
+    const float2 v = spec[e];
+    spec[e] = make_float2(v.x * K, v.y * K);
+  }
 }
 
 // Adjoint z pass: ct_s = c2r(V); per element the source adjoint.

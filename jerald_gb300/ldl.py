@@ -27,6 +27,11 @@ _MODES = {"reference": 0, "true": 1}
 _PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 
 
+class _LossExt(ct.Structure):
+    """jld_ldl_loss_ext of include/jld.h."""
+    _fields_ = [("n", ct.c_float), ("index", ct.c_float), ("field2", ct.c_void_p), ("maskvalid", ct.c_void_p)]
+
+
 def _new_graph():
     """A CUDA graph whose cudaGraph_t stays queryable after instantiation
     (for counting its kernel nodes) where torch supports that."""
@@ -49,7 +54,7 @@ def _finish_capture(g) -> None:
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
                  grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
-                 pipelined: bool = True, recompute: bool = False):
+                 pipelined: bool = True, recompute: bool = False, n: float = 0.0, index: float = 1.0):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
         self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
@@ -70,7 +75,13 @@ class FusedLDL:
         if nbytes == 0:
             raise ValueError("invalid fused-step geometry")
         self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
-        self.out = torch.zeros(1 + self.nparams, dtype=torch.float64, device=self.device)
+        if not (n >= 0):
+            raise ValueError("n must be >= 0")
+        self.n = float(n)          # loss smoothing exponent (model.py:376-381)
+        self.index = float(index)  # map exponent (model.py:357)
+        # [loss, grads..., validation loss]; `out` is the [loss, grads...] view
+        self._buf = torch.zeros(2 + self.nparams, dtype=torch.float64, device=self.device)
+        self.out = self._buf[:1 + self.nparams]
         self.params = torch.zeros(self.nparams, dtype=torch.float32, device=self.device)
         with torch.cuda.device(self.device):
             _lib.call("jld_ldl_prepare_f32", *self.nmesh, self.box.ctypes.data_as(ct.c_void_p))
@@ -86,20 +97,29 @@ class FusedLDL:
     def workspace_bytes(self) -> int:
         return self.ws.numel()
 
-    def _launch(self, pos: torch.Tensor, target: torch.Tensor, mask):
+    def _launch(self, pos: torch.Tensor, target: torch.Tensor, mask, field2=None, maskvalid=None):
         if pos.dtype != torch.float32 or not pos.is_contiguous() or pos.shape != (self.nparts, 3):
             raise ValueError("pos must be a contiguous float32 (nparts, 3) CUDA tensor")
-        if target.dtype != torch.float32 or not target.is_contiguous() or target.numel() != np.prod(self.nmesh):
+        C = int(np.prod(self.nmesh))
+        if target.dtype != torch.float32 or not target.is_contiguous() or target.numel() != C:
             raise ValueError("target must be a contiguous float32 mesh")
-        if mask is not None and (mask.dtype != torch.float32 or not mask.is_contiguous()):
-            raise ValueError("mask must be a contiguous float32 mesh")
+        for name, m in (("mask", mask), ("field2", field2), ("maskvalid", maskvalid)):
+            if m is not None and (m.dtype != torch.float32 or not m.is_contiguous() or m.numel() != C):
+                raise ValueError(f"{name} must be a contiguous float32 mesh")
+        ptr = lambda t: ct.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        ext = _LossExt(self.n, self.index, ptr(field2), ptr(maskvalid))
         st = ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
-        _lib.call("jld_ldl_step_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
+        _lib.call("jld_ldl_step_ext_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
                   self.box.ctypes.data_as(ct.c_void_p), self.nstep, _KINDS[self.kind], int(self.L1),
                   _MODES[self.grad_mode], self.options,
-                  ct.c_void_p(self.params.data_ptr()),
-                  ct.c_void_p(target.data_ptr()), ct.c_void_p(mask.data_ptr()) if mask is not None else None,
-                  ct.c_void_p(self.ws.data_ptr()), self.ws.numel(), ct.c_void_p(self.out.data_ptr()))
+                  ct.c_void_p(self.params.data_ptr()), ct.c_void_p(target.data_ptr()), ptr(mask),
+                  ct.c_void_p(ct.addressof(ext)), ct.c_void_p(self.ws.data_ptr()), self.ws.numel(),
+                  ct.c_void_p(self._buf.data_ptr()))
+
+    @property
+    def lossv(self) -> torch.Tensor:
+        """Validation loss of the last step (model.py lossv; 0 without maskvalid)."""
+        return self._buf[1 + self.nparams]
 
     def _set_params(self, params):
         p = torch.as_tensor(params, dtype=torch.float32).reshape(-1)
@@ -107,30 +127,31 @@ class FusedLDL:
             raise ValueError(f"expected {self.nparams} parameters, got {p.numel()}")
         self.params.copy_(p.to(self.device), non_blocking=True)
 
-    def __call__(self, pos, params, target, mask=None):
-        """Eager step; returns (loss, grad) as float64 device tensors."""
+    def __call__(self, pos, params, target, mask=None, field2=None, maskvalid=None):
+        """Eager step; returns (loss, grad) as float64 device tensors (the
+        validation loss is `lossv`)."""
         self._set_params(params)
-        self._launch(pos, target, mask)
+        self._launch(pos, target, mask, field2, maskvalid)
         return self.out[0], self.out[1:]
 
-    def capture_graph(self, pos, target, mask=None):
+    def capture_graph(self, pos, target, mask=None, field2=None, maskvalid=None):
         """A new CUDA graph of the step on these (static) inputs; the step's
         own graph is left as it is."""
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
-            self._launch(pos, target, mask)  # builds plans, tables and kernel attributes
+            self._launch(pos, target, mask, field2, maskvalid)  # builds plans, tables and kernel attributes
         torch.cuda.current_stream(self.device).wait_stream(s)
         g = _new_graph()
         with torch.cuda.graph(g):
-            self._launch(pos, target, mask)
+            self._launch(pos, target, mask, field2, maskvalid)
         _finish_capture(g)
         return g
 
-    def capture(self, pos, target, mask=None):
+    def capture(self, pos, target, mask=None, field2=None, maskvalid=None):
         """Captures the step on static inputs (they must stay alive and in place)."""
-        self._static = (pos, target, mask)
-        self.graph = self.capture_graph(pos, target, mask)
+        self._static = (pos, target, mask, field2, maskvalid)
+        self.graph = self.capture_graph(pos, target, mask, field2, maskvalid)
         return self.graph
 
     def replay(self, params=None):

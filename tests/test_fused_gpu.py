@@ -257,3 +257,75 @@ def test_host_feed_matches_eager_steps():
         # small difference of large sums, so allow 1e-3 per component
         assert _rel(out[k, 1:].numpy(), go.cpu().numpy()).max() < 1e-3
     assert float(out[0, 0]) != float(out[1, 0])
+
+
+@pytest.mark.parametrize("case", ["sm_smooth_L1", "sm_smooth_L2_masks", "sm_index_field2_valid", "dm_smooth_L2"])
+@pytest.mark.parametrize("mode", ["reference", "true"])
+def test_fused_loss_options_match_plain_f64(case, mode):
+    """The rest of model.py's loss in the fused step -- residual smoothing by
+    |k|^-n + 1, the map exponent and second field, the validation loss --
+    against the FP64 plain path on the same inputs (loss and validation loss
+    within 1e-5, gradient 1e-3 norm-wise and 1e-2 per component) and the loss
+    against the FP64 oracle's forward (1e-5)."""
+    from jerald_gb300 import jaxpops_bind as jpo
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    from jerald_gb300.model import JERALDModel
+    from jerald_gb300.pmesh import PMesh
+    from oracle.ldl import model_loss
+    n, box = 32, 100.0
+    rng = np.random.default_rng(5)
+    X = synth.zeldovich(n, box, 0.5, seed=6, dtype=np.float32).astype(np.float64)
+    kind = "dm" if case.startswith("dm") else "sm"
+    p = synth.default_params(2)[:10 if kind == "dm" else 13]
+    tgt = rng.uniform(0.5, 1.5, (n,) * 3)
+    if kind == "dm":
+        # the dm map has mean 1 whatever the parameters (the paint conserves
+        # mass), so a residual with a nonzero mean would put the loss in the
+        # k = 0 mode, weighted (1e-8)^-n + 1, whose gradient is exactly zero
+        # and drowns the rest in float32: give the target mean 1 as well
+        tgt /= tgt.mean()
+    tgt = tgt.astype(np.float32)
+    L1 = "L1" in case
+    o = dict(n=0.0, index=1.0, field2=None, mask=None, maskvalid=None)
+    if "smooth" in case:
+        # the k = 0 weight (1e-8)^-n + 1 multiplies the float32 rounding of
+        # the residual's mean: 1e2 at n = 0.25, 1e4 at 0.5, 1e8 at 1
+        o["n"] = 0.25 if kind == "dm" else 0.5
+    if "masks" in case or "valid" in case:
+        o["mask"] = rng.integers(0, 2, (n,) * 3).astype(np.float32)
+        o["maskvalid"] = (1.0 - o["mask"]).astype(np.float32)
+    if "index" in case:
+        o["index"] = 2.0
+        o["field2"] = rng.uniform(0.8, 1.2, (n,) * 3).astype(np.float32)
+    ref, refv = model_loss((n,) * 3, box, kind, p, X, tgt.astype(np.float64), 2, L1=L1, n=o["n"], index=o["index"],
+                           field2=o["field2"], mask=o["mask"], maskvalid=o["maskvalid"])
+    d32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda() if a is not None else None  # noqa
+    d64 = lambda a: torch.from_numpy(np.asarray(a, dtype=np.float64)).cuda() if a is not None else None  # noqa
+    f = FusedLDL(n, box, len(X), nstep=2, kind=kind, L1=L1, grad_mode=mode, n=o["n"], index=o["index"])
+    loss, g = f(d32(X), p, d32(tgt), d32(o["mask"]), d32(o["field2"]), d32(o["maskvalid"]))
+    torch.cuda.synchronize()
+    loss, lossv, g = float(loss), float(f.lossv), g.cpu().numpy()
+    pm = PMesh(n, box, dtype=torch.float64)
+    model = JERALDModel(d64(X), d64(tgt), pm, Nstep=2, kind=kind, L1=L1, n=o["n"], index=o["index"],
+                        field2=d64(o["field2"]), masktrain=d64(o["mask"]), maskvalid=d64(o["maskvalid"]))
+    jpo.set_fft_adjoint(mode)
+    try:
+        lp, lvp, gp = model.lossv_and_grad(torch.from_numpy(p))
+    finally:
+        jpo.set_fft_adjoint("reference")
+    gp = gp.cpu().numpy()
+    assert abs(loss - ref) <= 1e-5 * abs(ref), (loss, ref)
+    assert abs(loss - float(lp)) <= 1e-5 * abs(float(lp))
+    if o["maskvalid"] is not None:
+        assert abs(lossv - refv) <= 1e-5 * abs(refv)
+        assert abs(lossv - float(lvp)) <= 1e-5 * abs(float(lvp))
+    else:
+        assert lossv == 0.0
+    assert np.linalg.norm(g - gp) / np.linalg.norm(gp) < 1e-3
+    assert _rel(g, gp).max() < 1e-2
+    # the same through a captured graph
+    f.capture(d32(X), d32(tgt), d32(o["mask"]), d32(o["field2"]), d32(o["maskvalid"]))
+    l2, g2 = f.replay(p)
+    torch.cuda.synchronize()
+    assert abs(float(l2) - loss) <= 1e-6 * abs(loss)
