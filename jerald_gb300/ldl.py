@@ -206,14 +206,17 @@ class HostFeed:
     with the host-to-device copies of step k+1 overlapped with the compute
     of step k: two device input buffers with one captured graph each, a copy
     stream and events.  Page-locked inputs are streamed in by a small kernel
-    that reads host memory directly (jld_copy_from_host); others go through
-    copy_.  Every step's positions and target are copied and its loss and
+    that reads host memory directly (jld_copy_from_host, copy="kernel") or
+    by the copy engines (copy="engine"); others go through copy_.  Every step's positions and target are copied and its loss and
     gradient are read back; only the order of the copies changes, not their
     amount.
     """
 
-    def __init__(self, step: FusedLDL, mask=None):
+    def __init__(self, step: FusedLDL, mask=None, copy: str = "kernel", ctas: int = 16):
+        if copy not in ("kernel", "engine"):
+            raise ValueError("copy must be 'kernel' or 'engine'")
         self.step = step
+        self.copy_mode = copy
         dev = step.device
         self.pos = [torch.empty((step.nparts, 3), dtype=torch.float32, device=dev) for _ in range(2)]
         self.tgt = [torch.empty(step.nmesh, dtype=torch.float32, device=dev) for _ in range(2)]
@@ -222,7 +225,7 @@ class HostFeed:
         self.mask = mask
         self.graphs = [step.capture_graph(self.pos[b], self.tgt[b], mask) for b in range(2)]
         self.copy = torch.cuda.Stream(dev)
-        self.ctas = 16  # enough to saturate the host link; leaves the SMs to the step
+        self.ctas = int(ctas)  # enough to saturate the host link; leaves the SMs to the step
         self.copied = [torch.cuda.Event() for _ in range(2)]
         self.free = [torch.cuda.Event() for _ in range(2)]
 
@@ -241,8 +244,8 @@ class HostFeed:
 
         def put(dst: torch.Tensor, src: torch.Tensor) -> None:
             nbytes = dst.numel() * dst.element_size()
-            if (src.is_pinned() and src.is_contiguous() and src.numel() == dst.numel()
-                    and src.dtype == dst.dtype and src.data_ptr() % 16 == 0):
+            if (self.copy_mode == "kernel" and src.is_pinned() and src.is_contiguous()
+                    and src.numel() == dst.numel() and src.dtype == dst.dtype and src.data_ptr() % 16 == 0):
                 # a few CTAs read the page-locked buffer directly (NVLink-C2C)
                 _lib.call("jld_copy_from_host", cs, ct.c_void_p(dst.data_ptr()), ct.c_void_p(src.data_ptr()),
                           nbytes, self.ctas)
