@@ -211,7 +211,7 @@ def _paint_case(case):
 @pytest.mark.parametrize("method", [0, 1])
 @pytest.mark.parametrize("case", ["exact_lattice", "lattice", "lattice_nz34", "lattice_nz33", "mixed",
                                   "ragged_edges"])
-def test_paint_methods_runs_and_windows(jl, method, case):
+def test_paint_methods_lattice_and_clumps(jl, method, case):
     pos, mass, nm, box = _paint_case(case)
     m = np.ones(len(pos), np.float32) if mass is None else mass
     ref = cic.paint(cic.box_to_mesh(pos, box, nm), m, nm)
