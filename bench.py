@@ -320,6 +320,89 @@ def run_batch(args):
     return 0
 
 
+def run_snapmap(args):
+    """Snapshot-map ingestion (makemap, JERALD/snaputils.py:253-406): N gas
+    particles in host memory (Coordinates, Masses, ElectronAbundance,
+    InternalEnergy: map kind nT, 24 bytes per particle) streamed in chunks of
+    2^23 onto an n^3 mesh; wall-clock particles/s and host bytes/s of the
+    whole call (host staging copy, host-to-device copies, weights and paint),
+    with the oracle's numpy restatement timed on a 1 % sample beside it."""
+    import time
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import types
+    from jerald_gb300 import snapmap
+    from oracle import snapmap as osm
+    N, n, box = int(args.snapmap), args.n, 25.0
+    rng = np.random.default_rng(0)
+    fields = {"Coordinates": (rng.random((N, 3), dtype=np.float32) * np.float32(box * 1000.0)),
+              "Masses": rng.random(N, dtype=np.float32) * np.float32(1e-3),
+              "ElectronAbundance": rng.random(N, dtype=np.float32) * np.float32(1.2),
+              "InternalEnergy": rng.random(N, dtype=np.float32) * np.float32(1e4)}
+    snap = snapmap.ArraySnapshot(redshift=2.0, parts={0: fields})
+    pm = types.SimpleNamespace(Nmesh=np.asarray([n] * 3), BoxSize=np.asarray([box] * 3), device="cuda",
+                               fftss=(0, n))
+    for _ in range(max(1, args.warmup - 2)):
+        snapmap.makemap(snap, "nT", pm, save=False, return_tensor=True)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        m = snapmap.makemap(snap, "nT", pm, save=False, return_tensor=True)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    sec = float(np.median(ts))
+    k = max(1, N // 100)
+    sample = {f: v[:k] for f, v in fields.items()}
+    t0 = time.perf_counter()
+    osm.makemap(sample, "nT", (n,) * 3, [box] * 3, 2.0)
+    cpu = (time.perf_counter() - t0) * (N / k)
+    print(json.dumps({"metric": "snapshot-map ingestion (makemap, kind nT)", "value": N / sec, "unit": "particles/s",
+                      "seconds": sec, "host_gbs": N * 28 / sec / 1e9, "nparts": N, "nmesh": n,
+                      "data": "synthetic uniform gas particles (seeded)", "map_sum": float(m.double().sum()),
+                      "cpu_baseline": {"value": N / cpu, "unit": "particles/s", "cores": 1, "kind": "port",
+                                       "sample": f"oracle numpy makemap on {k} particles, scaled"}}), flush=True)
+    return 0
+
+
+def run_loss_ext(args):
+    """The fused step with the rest of model.py's loss (smoothing n = 0.5 of
+    the residual, a validation mask) next to the plain-loss step on the same
+    workload: ms per step of each."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    dev = torch.device("cuda", 0)
+    n = args.n
+    params = synth.default_params(2)
+    pos, box = make_workload(n, dev)
+    target = make_target(pos, n, box, params, dev)
+    mv = torch.from_numpy(np.random.default_rng(3).integers(0, 2, (n,) * 3).astype(np.float32)).to(dev)
+    out = {"workload": f"clustered {n}^3, 2 sm layers, L1 loss", "nmesh": n}
+    for name, kw, extra in (("plain_loss", {}, {}), ("smooth_0.5_valid", {"n": 0.5}, {"maskvalid": mv})):
+        step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, device=dev, **kw)
+        step(pos, params, target, **extra)
+        step.capture(pos, target, **extra)
+        for _ in range(args.warmup):
+            step.replay(params)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            step.replay(params)
+        e1.record(st)
+        torch.cuda.synchronize()
+        out[name] = {"ms_per_step": e0.elapsed_time(e1) / args.steps, "loss": float(step.out[0]),
+                     "lossv": float(step.lossv), "graph_kernels": step.graph_kernels()}
+        del step
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_precision(args):
     """Fused FP32 step vs the FP64 primitive pipeline (plain JERALDModel in
     float64 on the same positions and target): loss and gradient errors."""
@@ -379,6 +462,10 @@ def main():
                     help="instead of the main workload: N boxes of mixed meshes in one graph (prints its own line)")
     ap.add_argument("--recompute", action="store_true",
                     help="memory plan: one force-mesh slot, recomputed in the adjoint")
+    ap.add_argument("--snapmap", type=int, default=0,
+                    help="instead of the main workload: makemap of N synthetic gas particles (prints its own line)")
+    ap.add_argument("--loss-ext", action="store_true",
+                    help="instead of the main workload: the fused step with residual smoothing and a validation mask")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -390,6 +477,10 @@ def main():
         return run_precision(args)
     if args.batch:
         return run_batch(args)
+    if args.snapmap:
+        return run_snapmap(args)
+    if args.loss_ext:
+        return run_loss_ext(args)
 
     import torch
     from jerald_gb300 import replicas

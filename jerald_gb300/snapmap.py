@@ -231,14 +231,17 @@ def makemap(path, kind, pm, f32=True, local=True, save=True, outpath=None, verbo
         s.used.record(comp)
     for i, ch in enumerate(snap.chunks(ptNum, fields, mdi, chunk)):
         s = slots[i % 2]
-        pos = _f32(ch["Coordinates"]).reshape(-1)
-        n = pos.size // 3
+        n = int(ch["Coordinates"].shape[0])
         if n == 0:
             continue
         s.used.synchronize()                       # the GPU is done with this slot's buffers
         for k in names:
-            v = _f32(ch[k]).reshape(-1)
-            s.host[k][:v.size].numpy()[...] = v
+            v = ch[k]
+            if isinstance(v, torch.Tensor):
+                v = v.reshape(-1)
+            else:
+                v = torch.from_numpy(_f32(v).reshape(-1))
+            s.host[k][:v.numel()].copy_(v)         # multi-threaded host copy into pinned staging
         with torch.cuda.stream(copy):
             for k in names:
                 m = n * (3 if k == "Coordinates" else 1)
