@@ -236,7 +236,7 @@ static FftPipe fft_pipe_geom(int nx, int ny, int nz, bool c2r) {
   const int64_t rows = (int64_t)nx * ny;
   f.py = pipe_geom(nx, ny, h, 1, 0);
   f.px = pipe_geom(nx, ny, h, 0, 0);
-  f.z = c2r ? zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8) : zpipe_geom(rows, h, 1, (size_t)h * 8);
+  f.z = c2r ? zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8) : zpipe_geom(rows, h, 1, (size_t)h * 8, 110 * 1024, kZr2cThreads);
   f.ok = f.py.ok && f.px.ok && f.z.ok && (c2r || f.px.ok);
   return f;
 }

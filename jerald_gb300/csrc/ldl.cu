@@ -248,11 +248,11 @@ static int ldl_step(const StepArgs& a) {
   const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
   ZPipeGeom zr2c, zc2r3, zadj, zr2c3;
   if (a.use_pipe) {
-    zr2c = zpipe_geom(rows, h, 1, (size_t)h * 8);
+    zr2c = zpipe_geom(rows, h, 1, (size_t)h * 8, 110 * 1024, kZr2cThreads);
     // ~100 registers per thread: 192 / 128-thread CTAs keep 3-5 resident per SM
-    zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8, 110 * 1024, 192);
-    zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8, 110 * 1024, 128);
-    zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16);
+    zc2r3 = zpipe_geom(rows, h, 3, (size_t)3 * (h + 1) * 8, 110 * 1024, kZc2r3Threads);
+    zadj = zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8, 110 * 1024, kZadjThreads);
+    zr2c3 = zpipe_geom(rows, h, 3, (size_t)2 * h * 16, 110 * 1024, kZr2c3Threads);
   }
   // the generic kernels then only cover the nyq plane
   SpecPass gxn = gx.sp, gyn = gy.sp;

@@ -13,6 +13,7 @@ namespace jld {
 // Inverse z pass of the forward: three c2r transforms (x, y, z force
 // channels) interleaved into the float4 mesh g4[row][z] = (gx, gy, gz, 0).
 // Lines 0..R-1 of a tile are channel x, R..2R-1 channel y, 2R..3R-1 z.
+constexpr int kZc2r3Threads = 192;  // CTA size cap of its geometry
 template <class Sch>
 __global__ void __launch_bounds__(512)
 zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, const float2* __restrict__ Gz,
@@ -75,8 +76,11 @@ zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, 
 // Last adjoint z pass: c2r of the source cotangent V, then per real value
 // rb = ct * gamma * base^(gamma-1) * fact (skipped when rb == nullptr) and
 // the d gamma partial sum ct * base^gamma * log(base), base = fact*rho+1e-8.
+// 128-thread CTAs capped at 80 registers, six per SM (at 128 registers
+// four): 29.96 against 30.30 ms per 512^3 step; five (96 registers) 30.07.
+constexpr int kZadjThreads = 128;
 template <class Sch>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(kZadjThreads, 6)
 zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restrict__ twr,
                      const float* __restrict__ rho_paint, const float* __restrict__ params, float fact,
                      float* __restrict__ rb, double* __restrict__ partials, const float2* __restrict__ tw,
@@ -149,8 +153,11 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
 // mesh gb4 (rows of 2h float4) into Ax, Ay and c_z(kz) * Az (main + nyq).
 // Lines 0..R-1 of a tile are channel x, R..2R-1 channel y, 2R..3R-1 z; all
 // three read the same staged float4 rows.
+// 192-thread CTAs capped at 96 registers so that three fit per SM (at
+// 128 registers only two did): 29.95 against 30.12 ms per 512^3 step.
+constexpr int kZr2c3Threads = 192;
 template <class Sch>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(kZr2c3Threads, 3)
 zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __restrict__ twr,
                   const float* __restrict__ cz, float2* __restrict__ Ax, float2* __restrict__ Ay,
                   float2* __restrict__ Az, const float2* __restrict__ tw, int* err) {

@@ -82,6 +82,7 @@ __device__ __forceinline__ int z_my_tiles(int ntiles) {
 // ---------------------------------------------------------------------------
 // Forward z pass (r2c) of real rows with the source map applied on load:
 // main[row][k] (k < h) and nyq[row] = X[h].
+constexpr int kZr2cThreads = 256;  // CTA size cap of its geometry
 template <class Sch, class Src>
 __global__ void __launch_bounds__(512)
 zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* __restrict__ twr,
