@@ -502,7 +502,7 @@ gather_vjp_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
 // Adjoint of layer l with the paint adjoint of layer l+1 folded in:
 //   v = Xbp + sum_c rb[c] grad w_c(Xn)     (gather_vjp_kernel's arithmetic;
 //                                           Xbp == nullptr: no partial)
-//   Xb = v + J^T v at X (GATHER), gb4 += scatter of v (bwd_particles_kernel)
+//   Xb = v + J^T v at X (GATHER), gb4 += scatter of v (float4 atomics)
 // Xn are the positions after layer l, X the positions before it.
 // Warps walk 32 consecutive particles; lanes merge shared z faces before
 // the float4 atomics (zpair32_flags).  Measured on the 512^3 clustered step:
