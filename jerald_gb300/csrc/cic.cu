@@ -62,10 +62,12 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 // Paint (single channel).  mass == nullptr => every particle weighs mscalar.
 // Warps walk 32 consecutive particles at a time (all lanes stay in the loop
 // for the shuffles); lanes whose stencils share a z face merge it before
-// the atomics (zpair32_flags).  Also measured and slower here: a 16 x 2
-// lane layout that pairs y faces as well (a scalar atomic costs less than
-// the extra shuffles and ballots), 8- and 16-byte vector atomics over the
-// z runs, and per-warp shared-memory windows for clumps.
+// the atomics (zpair32_flags); batches whose stencils fall in a 4 x 4 x 4
+// cell window (halo clumps) go through a shared-memory window instead.
+// Also measured and slower here: a 16 x 2 lane layout that pairs y faces as
+// well (a scalar atomic costs less than the extra shuffles and ballots), 8-
+// and 16-byte vector atomics over the z runs, and 8 x 8 x 8 windows kept
+// across a warp's batches.
 // Six CTAs of 256 threads per SM in single precision (40 registers): on the
 // 512^3 clustered step five and six tie, seven and eight (32 registers, full
 // occupancy) are 0.7 ms slower, more warps queueing on the same atomics.
@@ -78,6 +80,14 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  // Clumps: a batch whose lower corners span at most three cells per axis
+  // adds its 8 x 32 corner values into a 4 x 4 x 4 shared-memory window
+  // first; the window then goes to the mesh with one atomic per nonzero
+  // cell, lanes on consecutive cells (few sectors per instruction, where
+  // the lanes' own atomics would touch a dozen).
+  __shared__ T wins[8][64];
+  T* win = wins[threadIdx.x >> 5];
+  const int nax[3] = {g.nx, g.ny, g.nz};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
     const int64_t p = base + lane;
@@ -98,6 +108,56 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
     for (int k = 0; k < 8; ++k) {
       int bits = corner_axis_bits(k);
       w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
+    }
+    // z span first: lattice-ordered batches (32 cells along z) leave here
+    {
+      unsigned mn[3], mx[3];
+      int ii[3];
+      bool clump = false;
+      ii[2] = (int)q[2];
+      mn[2] = __reduce_min_sync(full, live ? (unsigned)ii[2] : 0xffffffffu);
+      mx[2] = __reduce_max_sync(full, live ? (unsigned)ii[2] : 0u);
+      if (mx[2] - mn[2] <= 2u) {
+        ii[0] = (int)q[0];
+        ii[1] = (int)q[1];
+        bool inr = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) inr = inr && (unsigned)ii[a] < (unsigned)nax[a];
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          mn[a] = __reduce_min_sync(full, live ? (unsigned)ii[a] : 0xffffffffu);
+          mx[a] = __reduce_max_sync(full, live ? (unsigned)ii[a] : 0u);
+        }
+        clump = __all_sync(full, inr || !live) && mx[0] - mn[0] <= 2u && mx[1] - mn[1] <= 2u;
+      }
+      if (clump) {
+        win[lane] = T(0);
+        win[lane + 32] = T(0);
+        __syncwarp();
+        if (live) {
+          const int wb = ((ii[0] - (int)mn[0]) * 4 + (ii[1] - (int)mn[1])) * 4 + (ii[2] - (int)mn[2]);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int bits = corner_axis_bits(k);
+            atomicAdd(win + wb + (bits & 1) * 16 + ((bits >> 1) & 1) * 4 + (bits >> 2), w[k]);
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int sl = lane + 32 * h;
+          const T v = win[sl];
+          if (v != T(0)) {
+            int gx = (int)mn[0] + (sl >> 4), gy = (int)mn[1] + ((sl >> 2) & 3), gz = (int)mn[2] + (sl & 3);
+            if (gx >= g.nx) gx -= g.nx;
+            if (gy >= g.ny) gy -= g.ny;
+            if (gz >= g.nz) gz -= g.nz;
+            atomicAdd(out + ((uint32_t)gx * (uint32_t)g.sx + (uint32_t)gy * (uint32_t)g.sy + (uint32_t)gz), v);
+          }
+        }
+        __syncwarp();
+        continue;
+      }
     }
     const Pairing pr = zpair32_flags(live ? pair_key(c, g) : kNoPair);
 #pragma unroll
