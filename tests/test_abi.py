@@ -63,3 +63,34 @@ def test_exports_are_c_symbols_only(libjld):
     syms = [l.split()[-1] for l in out.splitlines() if " T " in l]
     ours = [s for s in syms if s.startswith("jld_")]
     assert set(declared_names()) <= set(ours)
+
+
+def test_argument_errors_before_any_launch(libjld):
+    """Argument checks of the newer entry points return a status and a
+    message before they touch the GPU (no device needed)."""
+    libjld.jld_last_error.restype = ct.c_char_p
+    box = (ct.c_double * 3)(25.0, 25.0, 25.0)
+    f = ct.c_void_p(16)  # never dereferenced: every call below fails first
+    sp = libjld.jld_snap_prep_f32
+    sp.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_float, ct.c_void_p, ct.c_int32] + \
+        [ct.c_void_p] * 5 + [ct.c_int64, ct.c_double, ct.c_double, ct.c_double, ct.c_double, ct.c_void_p,
+                             ct.c_void_p]
+    args = lambda kind, n=10, masses=f, unit=1000.0, b=box: (None, f, n, unit, b, kind, masses, f, f, f, f, 3,  # noqa
+                                                              1.0, 1.0, 0.76, 1.0, f, f)
+    assert sp(*args(8)) == 1 and b"kind" in libjld.jld_last_error()
+    assert sp(*args(2, masses=None)) == 1 and b"NULL" in libjld.jld_last_error()
+    assert sp(*args(2, n=-1)) == 1
+    assert sp(*args(2, unit=0.0)) == 1 and b"unit" in libjld.jld_last_error()
+    assert sp(*args(2, b=None)) == 1 and b"box" in libjld.jld_last_error()
+    assert sp(*args(2, n=0)) == 0  # nothing to do
+    ext = libjld.jld_ldl_step_ext_f32
+    ext.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
+                    ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_void_p,
+                    ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+    fbox = (ct.c_float * 3)(1.0, 1.0, 1.0)
+    assert ext(None, f, 8, 4, 4, 4, fbox, 2, 0, 1, 0, 0, f, f, None, None, f, 1 << 30, f) == 1
+    assert b"ext is NULL" in libjld.jld_last_error()
+    acc = libjld.jld_ppaint_box_acc_f32
+    acc.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_float, ct.c_int32, ct.c_int32,
+                    ct.c_int32, ct.c_void_p, ct.c_void_p]
+    assert acc(None, f, 8, None, ct.c_float(1.0), 4, 4, 4, None, f) == 1 and b"box" in libjld.jld_last_error()

@@ -92,3 +92,30 @@ def test_snapshot_host_logic(tmp_path):
     ch = list(snap.chunks(0, ["Coordinates", "Velocities"], [None, 2], 4))
     assert [len(c["Coordinates"]) for c in ch] == [4, 4, 2]
     np.testing.assert_array_equal(np.concatenate([c["Velocities"] for c in ch]), np.arange(2, 30, 3))
+
+
+def test_snapmap_oracle_known_answers():
+    """The oracle's makemap on single particles: a particle on a grid point
+    puts its whole weight in that cell; coordinates in kpc/h wrap into the
+    box; each kind's weight follows snaputils.py:360-376."""
+    from oracle import snapmap as osm
+    nm, box, z = (8, 8, 8), 4.0, 1.0
+    a, c1, c2 = osm.coefficients(z, [box] * 3, nm, h=0.7, XH=0.76)
+    assert a == 0.5 and c1 == 4.0475e-07 * 0.7 ** 2 / 0.5 ** 3 * 0.76 / box ** 3 * 8 ** 3
+    cell = box / 8
+    # grid point (3, 1, 6) given once inside and once a box length away
+    for shift in (0.0, box, -box):
+        coords = np.array([[(3 * cell + shift) * 1000.0, 1 * cell * 1000.0, 6 * cell * 1000.0]], np.float32)
+        f = {"Coordinates": coords, "Masses": np.array([2e-3], np.float32),
+             "ElectronAbundance": np.array([1.1], np.float32), "InternalEnergy": np.array([500.0], np.float32),
+             "NeutralHydrogenAbundance": np.array([0.25], np.float32), "Velocities": np.array([-120.0], np.float32)}
+        expect = {"ne": c1 * np.float32(2e-3) * np.float32(1.1),
+                  "nT": c1 * np.float32(2e-3) * np.float32(1.1) * c2 * np.float32(500.0)
+                  / (1 + 3 * 0.76 + 4 * 0.76 * np.float32(1.1)),
+                  "nHI": c1 * np.float32(2e-3) * np.float32(0.25),
+                  "MstarVz": np.float32(2e-3) * np.float32(-120.0) * a ** 0.5,
+                  "XHI": np.float32(0.25), "Mstar": np.float32(2e-3), "dm": 8.0 ** 3}
+        for kind, w in expect.items():
+            m = osm.makemap(f, kind, nm, [box] * 3, z, h=0.7, XH=0.76)
+            assert np.count_nonzero(m) == 1, (kind, shift)
+            assert m[3, 1, 6] == pytest.approx(float(np.float32(w)), rel=1e-6), kind
