@@ -36,8 +36,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() \
-    else "LDL fwd+grad steps/s at 512^3"
+METRIC = "LDL fwd+grad steps/s at 512³ (fused vs plain GPU ops, grad err≤1e-4); HBM %peak"
 UNIT = "steps/s"
 
 
