@@ -194,13 +194,12 @@ def count_launches(nstep: int, kind: str, mask: bool, recompute: bool = False) -
     return 1 + fwd + final + adj + rec
 
 
-def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int | None = None):
-    """Times the oracle's 2-layer fwd+grad at n_sample^3 (clustered recipe)."""
+def _oracle_case(n_sample: int, threads: int):
+    """The oracle's 2-layer fwd+grad set up at n_sample^3 (clustered recipe)."""
     from jerald_gb300 import synth
     from oracle import fft as offt
     from oracle import cic as ocic
     from oracle.ldl import LDLOracle
-    threads = threads or os.cpu_count() or 1
     offt.set_workers(threads)
     ocic.set_threads(threads)
     box = 100.0 * n_sample / 64
@@ -209,12 +208,10 @@ def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int
     o = LDLOracle((n_sample,) * 3, box, kind="sm", L1=True)
     o.forward(p, X, np.ones((n_sample,) * 3), 2)
     tgt = o.cache["F"] * synth.lognormal_noise(o.cache["F"].shape, 0.1, 2)
-    o.loss_and_grad(p, X, tgt, 2)  # warm
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        o.loss_and_grad(p, X, tgt, 2)
-    dt = (time.perf_counter() - t0) / steps
-    n_part_sample = len(X)
+    return (lambda: o.loss_and_grad(p, X, tgt, 2)), len(X)
+
+
+def _oracle_line(n_sample: int, n_full: int, threads: int, dt: float, n_part_sample: int):
     n_part_full = int(round(1.1 * n_full ** 3))
     value = (1.0 / dt) * n_part_sample / n_part_full
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
@@ -224,27 +221,44 @@ def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int
                       f"scaled by particle count to {n_full}^3"}
 
 
+def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int | None = None):
+    """Times the oracle's 2-layer fwd+grad at n_sample^3 (clustered recipe)."""
+    threads = threads or os.cpu_count() or 1
+    step, npart = _oracle_case(n_sample, threads)
+    step()  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    return _oracle_line(n_sample, n_full, threads, (time.perf_counter() - t0) / steps, npart)
+
+
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's CPU ops (the
+    reference itself needs MPI, FFTW and JAX, none of which exist here or
+    on the GPU machine) on all host threads, W untimed and K timed steps of a
+    128^3 sample of the workload, scaled by particle count."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     n_full = args.n
     n_sample = max(16, min(128, n_full))
-    cb = cpu_baseline_sample(n_sample, n_full, steps=1)
-    vals = []
-    from jerald_gb300 import synth  # noqa: F401
+    threads = os.cpu_count() or 1
+    step, npart = _oracle_case(n_sample, threads)
     for _ in range(args.warmup):
-        pass
+        step()
+    dts = []
     for _ in range(args.steps):
-        r = cpu_baseline_sample(n_sample, n_full, steps=1)
-        vals.append(r["value"])
-    v = float(np.median(vals)) if vals else cb["value"]
+        t0 = time.perf_counter()
+        step()
+        dts.append(time.perf_counter() - t0)
+    cb = _oracle_line(n_sample, n_full, threads, float(np.median(dts)), npart)
+    v = cb["value"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
             "config": {"workload": f"clustered {n_full}^3 particles+10% halos, {n_full}^3 mesh, 2 sm layers",
                        "nmesh": n_full},
-            "cpu_baseline": {**cb, "value": v},
+            "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
