@@ -187,3 +187,30 @@ def test_model_loss_matches_pipeline_forward():
         a = o.forward(p, X, tgt, 2)
         b, _ = model_loss((n,) * 3, box, kind, p, X, tgt, 2)
         assert abs(a - b) <= 1e-12 * abs(a)
+
+
+def test_model_loss_smoothing_known_answer():
+    """A residual that is the same constant c in every cell has only a k = 0
+    mode; the smoothing kernel weights it (1e-8)^-n + 1 (|k| = 0 is read as
+    1e-8, model.py:100-102), so the smoothed residual is c times that weight
+    everywhere: L1 loss |c| ((1e-8)^-n + 1), L2 its square; the validation
+    mask takes the same values over its own cells."""
+    import numpy as np
+    from oracle.ldl import model_loss
+    n, box = 8, 10.0
+    g = (np.arange(n) + 0.0) * box / n
+    X = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)  # one particle per cell corner
+    p = np.array([0.0, 1.0, 0.5, 2.0, 1.0] * 2)                           # alpha = 0: no displacement
+    c = 0.25
+    tgt = np.full((n,) * 3, 1.0 - c)                                      # dm map is 1 in every cell
+    for nn in (0.25, 0.5):
+        K0 = (1e-8) ** (-nn) + 1.0
+        l1, _ = model_loss((n,) * 3, box, "dm", p, X, tgt, 2, n=nn, L1=True)
+        assert abs(l1 - c * K0) <= 1e-9 * c * K0
+        mv = np.zeros((n,) * 3)
+        mv[:2] = 1.0
+        l2, lv = model_loss((n,) * 3, box, "dm", p, X, tgt, 2, n=nn, L1=False, maskvalid=mv)
+        assert abs(l2 - (c * K0) ** 2) <= 1e-9 * (c * K0) ** 2
+        assert abs(lv - (c * K0) ** 2) <= 1e-9 * (c * K0) ** 2
+    l0, _ = model_loss((n,) * 3, box, "dm", p, X, tgt, 2, n=0, L1=True)
+    assert abs(l0 - c) <= 1e-12
