@@ -15,8 +15,8 @@ weights (jld_snap_prep_f32) and the accumulating paint adds it to the map
 Sources of chunks:
   * HDF5Snapshot reads the reference's snapshot files (snapshot path
     resolution of snaputils.fname, the header, PartType<k>/<field>
-    datasets).  It needs h5py, which this environment does not have, so it
-    is not exercised by the tests here.
+    datasets).  It needs h5py, which this environment does not have: the
+    tests run its logic against an in-memory stand-in, not real files.
   * ArraySnapshot wraps in-memory arrays (any other reader, synthetic data).
 Positions and fields are float32 (the reference's default f32=True).
 """

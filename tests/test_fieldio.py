@@ -119,3 +119,62 @@ def test_snapmap_oracle_known_answers():
             m = osm.makemap(f, kind, nm, [box] * 3, z, h=0.7, XH=0.76)
             assert np.count_nonzero(m) == 1, (kind, shift)
             assert m[3, 1, 6] == pytest.approx(float(np.float32(w)), rel=1e-6), kind
+
+
+def test_hdf5_snapshot_reader_logic_with_a_stub(tmp_path, monkeypatch):
+    """HDF5Snapshot against an in-memory stand-in for h5py (absent here):
+    header attributes, files walked in order, files without the particle type
+    skipped, chunks split at max_particles, Velocities reduced to vz."""
+    import sys
+    import types as _types
+    from jerald_gb300 import snapmap
+    base = tmp_path / "snap_007"
+    nfile = 3
+    rng = np.random.default_rng(4)
+    files = {}
+    for i in range(nfile):
+        n = [5, 0, 7][i]
+        parts = {} if n == 0 else {"PartType0": {"Coordinates": rng.random((n, 3)) * 1e4,
+                                                  "Masses": rng.random(n),
+                                                  "Velocities": rng.standard_normal((n, 3))}}
+        npart = [n, 0, 0, 0, 0, 0]
+        files[f"{base}.{i}.hdf5"] = {"Header": {"Time": 0.5, "Redshift": 1.0, "BoxSize": 10000.0,
+                                                "NumFilesPerSnapshot": nfile, "Omega0": 0.3, "OmegaLambda": 0.7,
+                                                "HubbleParam": 0.7, "MassTable": [0.0] * 6,
+                                                "NumPart_ThisFile": npart, "NumPart_Total": [12, 0, 0, 0, 0, 0],
+                                                "Flag_Cooling": 1}, **parts}
+        (tmp_path / f"snap_007.{i}.hdf5").write_bytes(b"")
+
+    class _Group(dict):
+        pass
+
+    class _File:
+        def __init__(self, path, mode="r"):
+            d = files[str(path)]
+            self._d = {k: v for k, v in d.items() if k != "Header"}
+            self._h = _types.SimpleNamespace(attrs=d["Header"])
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+        def close(self):
+            pass
+
+        def __contains__(self, k):
+            return k == "Header" or k in self._d
+
+        def __getitem__(self, k):
+            return self._h if k == "Header" else _Group(self._d[k])
+
+    monkeypatch.setitem(sys.modules, "h5py", _types.SimpleNamespace(File=_File))
+    snap = snapmap.HDF5Snapshot(str(base))
+    assert snap.redshift == 1.0 and list(snap.nall) == [12, 0, 0, 0, 0, 0]
+    fields, mdi = snapmap.map_fields("neVz")[0][:2] + ["Velocities"], [None, None, 2]
+    got = list(snap.chunks(0, fields, mdi, 4))
+    assert [len(c["Coordinates"]) for c in got] == [4, 1, 4, 3]
+    want_v = np.concatenate([files[f"{base}.{i}.hdf5"]["PartType0"]["Velocities"][:, 2] for i in (0, 2)])
+    np.testing.assert_allclose(np.concatenate([c["Velocities"] for c in got]), want_v.astype(np.float32))
+    assert all(c["Masses"].dtype == np.float32 for c in got)
