@@ -241,8 +241,9 @@ JLD_API int jld_pifft_c_f64(jld_stream_t stream, const void* in_c, int32_t nx, i
 /* Limits: nx * ny * (nz/2 + 1) * 8 bytes <= 72 MiB (256^3 fits) and each */
 /* size <= 4096; larger meshes return JLD_ERR_WORKSPACE / UNSUPPORTED.     */
 /* The first call on a device resolves the arrays' addresses (make it      */
-/* before any stream capture).  All calls share the arrays: calls that     */
-/* overlap on the GPU race.                                                */
+/* before any stream capture).  All calls share the arrays and rewrite    */
+/* both (the twiddle table for their shape, the scratch by their passes): */
+/* calls that overlap on the GPU race on either.                           */
 JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_t nx,
                                   int32_t ny, int32_t nz, void* out_c);
 
@@ -280,6 +281,15 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /* the last reset is invalid); reset != 0 clears it.  No counterpart in    */
 /* the reference.                                                          */
 JLD_API int jld_fft_pipe_status(int32_t* value, int32_t reset);
+/* Error-path check of the bounded device waits (no counterpart in the    */
+/* reference, whose custom calls have no error channel: a `throw` inside  */
+/* a void call, lib/parops_fast.h:186).  One CTA arms an mbarrier for a    */
+/* copy that is never issued, polls it `polls` times (1 .. 2^22) with the  */
+/* pipelined passes' bounded wait, gives up, writes 99 to `word` and       */
+/* returns; no copy is in flight.  word == NULL: the pipelined FFT error   */
+/* word (read it with jld_fft_pipe_status); otherwise a device int, e.g.   */
+/* the fused step's word from jld_ldl_error_word_f32.                      */
+JLD_API int jld_wait_selftest(jld_stream_t stream, int32_t polls, int32_t* word);
 /* Workspace bytes for the given option bits (0 for invalid arguments);    */
 /* jld_ldl_workspace_f32 is the size for options = 4, enough for any      */
 /* option set without bit 3.  No counterpart in the reference (its        */

@@ -71,6 +71,7 @@ _SIGS = {
     "jld_graph_kernel_nodes": [_c_void_p, _c_void_p],
     "jld_copy_from_host": [_c_void_p, _c_void_p, _c_void_p, _size, _i32],
     "jld_fft_pipe_status": [_c_void_p, _i32],
+    "jld_wait_selftest": [_c_void_p, _i32, _c_void_p],
 }
 _RESTYPES = {
     "jld_version": ct.c_char_p,

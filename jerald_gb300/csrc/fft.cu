@@ -224,6 +224,37 @@ static int fft_err_word(int** out) {
 
 static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// Error-path check of the bounded waits: an mbarrier armed for 16 bytes of
+// a copy that is never issued, so its phase cannot complete.  The CTA polls
+// it with the same bounded wait as the pipelined passes, gives up after
+// `polls` tries, records kWaitSelftestCode in `word` and returns.  Nothing is
+// in flight, so giving up touches no memory but the word.
+constexpr int kWaitSelftestCode = 99;
+__global__ void __launch_bounds__(32) wait_selftest_kernel(int polls, int* word) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar, 16);
+  __syncthreads();
+  const bool done = mbar_wait_bounded(&bar, 0, polls);
+  if (!__syncthreads_or(done) && threadIdx.x == 0) atomicExch(word, kWaitSelftestCode);
+}
+
+static int wait_selftest(cudaStream_t st, int polls, int* word) {
+  if (polls < 1 || polls > kWaitLimit)
+    return set_error(JLD_ERR_ARG, "jld_wait_selftest: polls must be in [1, %d]", kWaitLimit);
+  if (!word) {
+    int s = fft_err_word(&word);
+    if (s) return s;
+  }
+  wait_selftest_kernel<<<1, 32, 0, st>>>(polls, word);
+  JLD_LAUNCH_CHECK("wait_selftest_kernel");
+  return JLD_OK;
+}
+
 struct FftPipe {
   bool ok = false;
   PipeGeom py, px;
@@ -411,9 +442,11 @@ static int irfft3(cudaStream_t st, const cplx_t<T>* in_c, const T* in_re, const 
 // stand-ins, not device addresses.  The first call on each device resolves
 // their device addresses with cudaGetSymbolAddress (with that device
 // current); make that first call before any stream capture.  Every call
-// shares the arrays and overwrites them (the scratch needs no clearing: each
-// pass writes all of it before it is read), so calls that overlap on the GPU
-// -- on two streams, or on one device from two threads -- race.
+// shares both arrays and rewrites both -- the twiddle table for its own
+// shape, the scratch by its passes (it needs no clearing: each pass writes
+// all of it before it is read) -- so calls that overlap on the GPU (on two
+// streams, or on one device from two threads) race on the twiddles as well
+// as on the scratch.
 static constexpr size_t kStaticScratchBytes = (size_t)72 << 20;
 static constexpr int kStaticMaxLen = 4096;
 static constexpr int kStaticTwLen = 2 * kStaticMaxLen + kStaticMaxLen / 2 + kStaticMaxLen / 2 + 1;
@@ -585,6 +618,11 @@ int jld_pfft_c_static_f32(jld_stream_t s, const float* data, int32_t nx, int32_t
                           void* out) {
   clear_error();
   return pfft_static_impl(ST(s), data, nx, ny, nz, (float2*)out);
+}
+
+JLD_API int jld_wait_selftest(jld_stream_t s, int32_t polls, int32_t* word) {
+  clear_error();
+  return wait_selftest(ST(s), polls, (int*)word);
 }
 
 JLD_API int jld_fft_pipe_status(int32_t* value, int32_t reset) {

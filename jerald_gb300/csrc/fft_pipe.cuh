@@ -53,9 +53,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 constexpr int kWaitLimit = 1 << 22;
 
-// Bounded wait on `parity` of an mbarrier; false after kWaitLimit polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < kWaitLimit; ++it)
+// Bounded wait on `parity` of an mbarrier; false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = kWaitLimit) {
+  for (int it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

@@ -60,9 +60,14 @@ snap_prep_kernel(const float* __restrict__ pos, int64_t n, float unit, double bx
       case 1: v = (double)__ldg(f.mass + p); break;
       case 2: v = c1 * (double)__ldg(f.mass + p) * (double)__ldg(f.xe + p); break;
       case 3: {
-        const double xe = (double)__ldg(f.xe + p);
-        const double den = __dadd_rn(__dadd_rn(1.0, __dmul_rn(3.0, XH)), __dmul_rn(__dmul_rn(4.0, XH), xe));
-        v = c1 * (double)__ldg(f.mass + p) * xe * c2 * (double)__ldg(f.u + p) / den;
+        // (1 + 3 * XH + 4 * XH * Xe) with XH a Python float and Xe a float32
+        // array is a float32 array under NumPy 2 promotion: the Python-float
+        // constants 1 + 3 XH and 4 XH are rounded to float32 once, the
+        // product and the sum are float32 operations.  The numerator has a
+        // float64 coefficient, so the quotient is float64.
+        const float xef = __ldg(f.xe + p);
+        const float den = __fadd_rn((float)(1.0 + 3.0 * XH), __fmul_rn((float)(4.0 * XH), xef));
+        v = c1 * (double)__ldg(f.mass + p) * (double)xef * c2 * (double)__ldg(f.u + p) / (double)den;
         break;
       }
       case 4: v = c1 * (double)__ldg(f.mass + p) * (double)__ldg(f.nhi + p); break;

@@ -94,3 +94,7 @@ def test_argument_errors_before_any_launch(libjld):
     acc.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_float, ct.c_int32, ct.c_int32,
                     ct.c_int32, ct.c_void_p, ct.c_void_p]
     assert acc(None, f, 8, None, ct.c_float(1.0), 4, 4, 4, None, f) == 1 and b"box" in libjld.jld_last_error()
+    ws = libjld.jld_wait_selftest
+    ws.argtypes = [ct.c_void_p, ct.c_int32, ct.c_void_p]
+    assert ws(None, 0, None) == 1 and b"polls" in libjld.jld_last_error()
+    assert ws(None, (1 << 22) + 1, None) == 1

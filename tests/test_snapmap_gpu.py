@@ -62,3 +62,34 @@ def test_makemap_saves_a_loadable_field(tmp_path):
     assert one.is_cuda and one.dtype == torch.float32
     # a second run adds in another atomic order
     assert np.abs(one.cpu().numpy() - out).max() <= 1e-5 * np.abs(out).max()
+
+
+@pytest.mark.parametrize("kind", ["Mstar", "ne", "nT", "nHI", "neVz", "MstarVz", "XHI"])
+def test_particle_weights_bit_exact(kind):
+    """The per-particle weights of jld_snap_prep_f32 equal NumPy's
+    (snaputils.py:360-376 under NumPy 2 promotion, cast to float32) bit for
+    bit, and the wrapped positions equal pos / 1000 % BoxSize."""
+    import ctypes as ct
+
+    from jerald_gb300 import _lib
+    from jerald_gb300.snapmap import KINDS
+    snap, box = _snapshot(seed=5, n=20000)
+    fields = dict(snap.parts[{"Mstar": 4, "MstarVz": 4}.get(kind, 0)])
+    vz = np.ascontiguousarray(fields["Velocities"][:, 2])
+    a, c1, c2 = osm.coefficients(2.3, [box] * 3, (32, 32, 32), h=0.7, XH=0.76)
+    want = np.asarray(osm.weights(kind, dict(fields, Velocities=vz), a, c1, c2, 0.76)).astype(np.float32)
+    want_pos = osm.positions(fields["Coordinates"], [box] * 3)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in fields.items()}
+    dvz = torch.from_numpy(vz).cuda()
+    n = len(want)
+    pos_out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    w = torch.empty(n, dtype=torch.float32, device="cuda")
+    P = lambda t: ct.c_void_p(t.data_ptr())  # noqa: E731
+    box64 = np.asarray([box] * 3, dtype=np.float64)
+    _lib.call("jld_snap_prep_f32", ct.c_void_p(torch.cuda.current_stream().cuda_stream), P(dev["Coordinates"]), n,
+              ct.c_float(1000.0), box64.ctypes.data_as(ct.c_void_p), KINDS[kind], P(dev["Masses"]),
+              P(dev["ElectronAbundance"]), P(dev["InternalEnergy"]), P(dev["NeutralHydrogenAbundance"]), P(dvz), 1,
+              float(c1), float(c2), 0.76, float(a ** 0.5), P(pos_out), P(w))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(w.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    np.testing.assert_array_equal(pos_out.cpu().numpy(), want_pos)
