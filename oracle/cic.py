@@ -35,6 +35,11 @@ def _ranges(n: int):
     return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:])]
 
 
+def _ranges_n(n: int, k: int):
+    edges = np.linspace(0, n, max(1, min(k, n)) + 1).astype(np.int64)
+    return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:])]
+
+
 def _pool_map(fn, ranges):
     if len(ranges) == 1:
         return [fn(*ranges[0])]
@@ -75,7 +80,8 @@ def box_to_mesh(pos: np.ndarray, box, nmesh) -> np.ndarray:
     out = np.empty_like(pos)
     b = np.ascontiguousarray(np.asarray(box, dtype=pos.dtype).reshape(3))
     nm = _nm(nmesh)
-    getattr(_load(), f"orc_box_to_mesh_{_sfx(pos)}")(_p(pos), ct.c_int64(len(pos)), _p(b), _p(nm), _p(out))
+    fn = getattr(_load(), f"orc_box_to_mesh_{_sfx(pos)}")
+    _pool_map(lambda a, e: fn(_p(pos[a:]), ct.c_int64(e - a), _p(b), _p(nm), _p(out[a:])), _ranges(len(pos)))
     return out
 
 
@@ -102,8 +108,12 @@ def paint(pos_mesh: np.ndarray, mass, nmesh) -> np.ndarray:
         return out
     meshes = _pool_map(part, _ranges(len(pos_mesh)))
     out = meshes[0]
-    for extra in meshes[1:]:
-        out += extra
+    if len(meshes) > 1:
+        # the range meshes are summed in range order, slab by slab in parallel
+        def add(a, e):
+            for extra in meshes[1:]:
+                out[a:e] += extra[a:e]
+        _pool_map(add, [(a, e) for a, e in _ranges_n(out.shape[0], len(meshes))])
     return out
 
 

@@ -37,6 +37,68 @@ from .fft import pfft, pifft
 
 PARAMS_PER_LAYER = 5  # alpha, gamma, kh, kl, nu (model.py:268-272)
 
+_EW = {"threads": 1}
+
+
+def set_threads(n: int) -> None:
+    """Host threads for the large elementwise expressions and sums (1 = plain
+    numpy, the default the tests use).  With n > 1 each expression runs on n
+    slabs along the first axis at once (numpy releases the GIL inside its
+    loops), which gives the same values; sums add n slab partials."""
+    _EW["threads"] = max(1, int(n))
+
+
+_POOL = {}
+
+
+def _pool(n):
+    if n not in _POOL:
+        from concurrent.futures import ThreadPoolExecutor
+        _POOL[n] = ThreadPoolExecutor(n)
+    return _POOL[n]
+
+
+def _slabs(length, n):
+    e = np.linspace(0, length, n + 1).astype(np.int64)
+    return [slice(int(a), int(b)) for a, b in zip(e[:-1], e[1:]) if b > a]
+
+
+def _ew(fn, *arrs):
+    """fn(*arrs) for an elementwise fn, evaluated slab by slab along axis 0
+    of the largest argument (arguments of another first extent are passed
+    whole and broadcast)."""
+    n = _EW["threads"]
+    big = max((a for a in arrs if isinstance(a, np.ndarray)), key=lambda a: a.size)
+    if n <= 1 or big.size < (1 << 20) or big.ndim == 0:
+        return fn(*arrs)
+    L = big.shape[0]
+    sl = _slabs(L, n)
+
+    def part(s):
+        return fn(*[a[s] if isinstance(a, np.ndarray) and a.ndim > 0 and a.shape[0] == L else a for a in arrs])
+    first = part(sl[0])
+    out = np.empty((L,) + first.shape[1:], dtype=first.dtype)
+    out[sl[0]] = first
+
+    def fill(s):
+        out[s] = part(s)
+    list(_pool(n).map(fill, sl[1:]))
+    return out
+
+
+def _sum(fn, *arrs):
+    """np.sum(fn(*arrs)), slab partials summed in slab order when threaded."""
+    n = _EW["threads"]
+    big = max((a for a in arrs if isinstance(a, np.ndarray)), key=lambda a: a.size)
+    if n <= 1 or big.size < (1 << 20) or big.ndim == 0:
+        return np.sum(fn(*arrs))
+    L = big.shape[0]
+
+    def part(s):
+        return np.sum(fn(*[a[s] if isinstance(a, np.ndarray) and a.ndim > 0 and a.shape[0] == L else a
+                           for a in arrs]))
+    return sum(_pool(n).map(part, _slabs(L, n)))
+
 
 def fftfreq_signed(n: int) -> np.ndarray:
     """Integer frequency index of numpy's fftfreq ordering."""
@@ -83,40 +145,43 @@ class LDLOracle:
         return cic.box_to_mesh(np.asarray(X, dtype=np.float64), self.box, self.nmesh)
 
     def green(self, kh, kl, nu):
-        k = self.knorm
         if self.kind == "dm":
-            return -np.exp(-k / kl - kh / k) * k ** nu
-        return -np.exp(-k ** 2 / kl ** 2 - kh ** 2 / k ** 2) * k ** nu
+            return _ew(lambda k: -np.exp(-k / kl - kh / k) * k ** nu, self.knorm)
+        return _ew(lambda k: -np.exp(-k ** 2 / kl ** 2 - kh ** 2 / k ** 2) * k ** nu, self.knorm)
 
     def green_grads(self, G, kh, kl, nu):
         """dG/dkh, dG/dkl, dG/dnu."""
         k = self.knorm
         if self.kind == "dm":
-            return G * (-1.0 / k), G * (k / kl ** 2), G * np.log(k)
-        return G * (-2.0 * kh / k ** 2), G * (2.0 * k ** 2 / kl ** 3), G * np.log(k)
+            return (_ew(lambda G, k: G * (-1.0 / k), G, k), _ew(lambda G, k: G * (k / kl ** 2), G, k),
+                    _ew(lambda G, k: G * np.log(k), G, k))
+        return (_ew(lambda G, k: G * (-2.0 * kh / k ** 2), G, k), _ew(lambda G, k: G * (2.0 * k ** 2 / kl ** 3), G, k),
+                _ew(lambda G, k: G * np.log(k), G, k))
 
     # -- forward --------------------------------------------------------------
     def layer_forward(self, X, prm, fact):
         alpha, gamma, kh, kl, nu = prm
         Xm = self.mesh_pos(X)
-        rho = cic.paint(Xm, 1.0, self.nmesh) * fact
-        s = (rho + 1e-8) ** gamma
-        shat = pfft(s) / self.ncell
+        rho = _ew(lambda r: r * fact, cic.paint(Xm, 1.0, self.nmesh))
+        s = _ew(lambda r: (r + 1e-8) ** gamma, rho)
+        shat = _ew(lambda v: v / self.ncell, pfft(s))
         G = self.green(kh, kl, nu)
-        P = 1e-2 * alpha * shat * G
-        g = [pifft(-1j * self.coeff[d] * P, self.nmesh) for d in range(3)]
-        disp = np.stack([cic.readout(Xm, g[d], self.nmesh, self.box) for d in range(3)], axis=-1)
+        P = _ew(lambda v, G: 1e-2 * alpha * v * G, shat, G)
+        g = [pifft(_ew(lambda c, P: -1j * c * P, self.coeff[d], P), self.nmesh) for d in range(3)]
+        disp = np.empty_like(X)
+        for d in range(3):
+            disp[:, d] = cic.readout(Xm, g[d], self.nmesh, self.box)
         c = dict(Xm=Xm, rho=rho, s=s, shat=shat, G=G, g=g, prm=prm)
-        return X + disp, c
+        return _ew(lambda a, b: a + b, X, disp), c
 
     def final_map(self, X, mu, w, b, fact):
         Xm = self.mesh_pos(X)
-        rho = cic.paint(Xm, 1.0, self.nmesh) * fact
+        rho = _ew(lambda r: r * fact, cic.paint(Xm, 1.0, self.nmesh))
         if self.kind == "dm":
             return rho, dict(Xm=Xm, rho=rho)
-        base = (rho + 1e-8) ** mu
-        u = w * base + b
-        F = np.where(u > 1e-12, u, 1e-12)
+        base = _ew(lambda r: (r + 1e-8) ** mu, rho)
+        u = _ew(lambda v: w * v + b, base)
+        F = _ew(lambda u: np.where(u > 1e-12, u, 1e-12), u)
         return F, dict(Xm=Xm, rho=rho, base=base, u=u)
 
     def forward(self, params, X, target, nstep, mask=None):
@@ -132,14 +197,14 @@ class LDLOracle:
         else:
             mu, w, b = params[5 * nstep: 5 * nstep + 3]
         F, fc = self.final_map(X, mu, w, b, fact)
-        diff = F - target
-        ad = np.abs(diff)
+        diff = _ew(lambda a, b: a - b, F, np.asarray(target, dtype=np.float64))
         if mask is not None:
-            ad = ad * mask
             npix = float(np.sum(mask))
+            ad = _ew(lambda d, m: np.abs(d) * m, diff, mask)
         else:
             npix = float(diff.size)
-        loss = (np.sum(ad) if self.L1 else np.sum(ad ** 2)) / npix
+            ad = _ew(np.abs, diff)
+        loss = (_sum(lambda a: a, ad) if self.L1 else _sum(lambda a: a ** 2, ad)) / npix
         self.cache = dict(layers=layers, final=fc, F=F, diff=diff, mask=mask, npix=npix,
                           fact=fact, params=params, nstep=nstep, X_final=X)
         return float(loss)
@@ -153,25 +218,23 @@ class LDLOracle:
         params, nstep, fact = c["params"], c["nstep"], c["fact"]
         grad = np.zeros_like(params)
         diff, mask, npix = c["diff"], c["mask"], c["npix"]
-        m = mask if mask is not None else 1.0
+        m = mask if mask is not None else np.float64(1.0)
         # d|diff|/d diff with JAX's abs rule (+1 at zero)
-        sgn = np.where(diff >= 0, 1.0, -1.0)
         if self.L1:
-            ctF = sgn * m / npix
+            ctF = _ew(lambda d, m: np.where(d >= 0, 1.0, -1.0) * m / npix, diff, m)
         else:
-            ctF = 2.0 * np.abs(diff) * m * m * sgn / npix
+            ctF = _ew(lambda d, m: 2.0 * np.abs(d) * m * m * np.where(d >= 0, 1.0, -1.0) / npix, diff, m)
         fc = c["final"]
         if self.kind == "dm":
             ct_rho = ctF
         else:
             mu, w, b = params[5 * nstep: 5 * nstep + 3]
-            ctu = ctF * (fc["u"] > 1e-12)
-            lr = np.log(fc["rho"] + 1e-8)
-            grad[5 * nstep + 0] = np.sum(ctu * w * fc["base"] * lr)
-            grad[5 * nstep + 1] = np.sum(ctu * fc["base"])
-            grad[5 * nstep + 2] = np.sum(ctu)
-            ct_rho = ctu * w * mu * (fc["rho"] + 1e-8) ** (mu - 1)
-        Xbar = cic.readout3d(fc["Xm"], ct_rho * fact, self.nmesh, self.box, vjp=True)
+            ctu = _ew(lambda f, u: f * (u > 1e-12), ctF, fc["u"])
+            grad[5 * nstep + 0] = _sum(lambda c, bs, r: c * w * bs * np.log(r + 1e-8), ctu, fc["base"], fc["rho"])
+            grad[5 * nstep + 1] = _sum(lambda c, bs: c * bs, ctu, fc["base"])
+            grad[5 * nstep + 2] = _sum(lambda c: c, ctu)
+            ct_rho = _ew(lambda c, r: c * w * mu * (r + 1e-8) ** (mu - 1), ctu, fc["rho"])
+        Xbar = cic.readout3d(fc["Xm"], _ew(lambda v: v * fact, ct_rho), self.nmesh, self.box, vjp=True)
         for l in reversed(range(nstep)):
             Xbar, g5 = self.layer_backward(c["layers"][l], Xbar, fact, mode)
             grad[5 * l: 5 * l + 5] = g5
@@ -183,33 +246,35 @@ class LDLOracle:
         Xbar = Xbar_next.copy()
         ct_g = []
         for d in range(3):
-            v = Xbar_next[:, d]
-            Xbar += cic.readout3d(Xm, g[d], self.nmesh, self.box, vjp=True) * v[:, None]
+            v = np.ascontiguousarray(Xbar_next[:, d])
+            Xbar = _ew(lambda a, r, v: a + r * v[:, None], Xbar,
+                       cic.readout3d(Xm, g[d], self.nmesh, self.box, vjp=True), v)
             ct_g.append(cic.paint(Xm, v, self.nmesh))
         ctP = np.zeros_like(lc["shat"])
         for d in range(3):
-            ctV = np.conj(pfft(ct_g[d]))
             if mode == "true":
-                ctV = ctV * self.mult
-            ctP += (-1j * self.coeff[d]) * ctV
+                ctP = _ew(lambda acc, c, V: acc + (-1j * c) * (np.conj(V) * self.mult), ctP, self.coeff[d],
+                          pfft(ct_g[d]))
+            else:
+                ctP = _ew(lambda acc, c, V: acc + (-1j * c) * np.conj(V), ctP, self.coeff[d], pfft(ct_g[d]))
         shat, G = lc["shat"], lc["G"]
-        ctw = G * ctP                                   # w = 1e-2 alpha shat
-        ctG = np.real(ctP * (1e-2 * alpha * shat))
+        ctw = _ew(lambda G, P: G * P, G, ctP)              # w = 1e-2 alpha shat
+        ctG = _ew(lambda P, s: np.real(P * (1e-2 * alpha * s)), ctP, shat)
         if mode == "reference":                          # c2f rule, model.py:23-29
             sz = ctG.shape[1]
             ctG[:, :, 1:sz // 2] *= 2.0
-        g_alpha = 1e-2 * np.sum(np.real(ctw * shat))
+        g_alpha = 1e-2 * _sum(lambda w, s: np.real(w * s), ctw, shat)
         dkh, dkl, dnu = self.green_grads(G, kh, kl, nu)
-        g_kh, g_kl, g_nu = np.sum(ctG * dkh), np.sum(ctG * dkl), np.sum(ctG * dnu)
-        ctF = (1e-2 * alpha) * ctw / self.ncell
+        g_kh, g_kl, g_nu = (_sum(lambda a, b: a * b, ctG, dkh), _sum(lambda a, b: a * b, ctG, dkl),
+                            _sum(lambda a, b: a * b, ctG, dnu))
         if mode == "reference":
-            cts = pifft(np.conj(ctF), self.nmesh)
+            cts = pifft(_ew(lambda w: np.conj((1e-2 * alpha) * w / self.ncell), ctw), self.nmesh)
         else:
-            cts = pifft(np.conj(ctF) / self.mult, self.nmesh)
+            cts = pifft(_ew(lambda w: np.conj((1e-2 * alpha) * w / self.ncell) / self.mult, ctw), self.nmesh)
         rho, s = lc["rho"], lc["s"]
-        g_gamma = np.sum(cts * s * np.log(rho + 1e-8))
-        ct_rho = cts * gamma * (rho + 1e-8) ** (gamma - 1)
-        Xbar += cic.readout3d(Xm, ct_rho * fact, self.nmesh, self.box, vjp=True)
+        g_gamma = _sum(lambda c, s, r: c * s * np.log(r + 1e-8), cts, s, rho)
+        ct_rho = _ew(lambda c, r: c * gamma * (r + 1e-8) ** (gamma - 1) * fact, cts, rho)
+        Xbar = _ew(lambda a, b: a + b, Xbar, cic.readout3d(Xm, ct_rho, self.nmesh, self.box, vjp=True))
         return Xbar, np.array([g_alpha, g_gamma, g_kh, g_kl, g_nu])
 
     def loss_and_grad(self, params, X, target, nstep, mask=None, mode="reference"):
