@@ -16,9 +16,12 @@ flush is needed between steps.  `e2e` repeats the step through the public
 API with host buffers: pinned-host -> device copies of positions and target
 and a device -> host read of loss and gradients inside the timed region.
 
---impl reference times the oracle's CPU restatement of the same step (C CIC
-loops, pocketFFT) on a bounded sample (a 128^3 version of the workload),
-scaled to the 512^3 workload by particle count.
+Both arms draw the same inputs: the positions are generated on the host
+(numpy, seeded) and copied to the device.  --impl reference times the
+oracle's FP64 CPU restatement of the same step (the reference's own ops need
+MPI, FFTW and JAX, which neither host has): C CIC loops over particle ranges
+and pocketFFT on every host thread, on the full workload, W untimed and K
+timed steps, with the same config as this arm.
 """
 from __future__ import annotations
 
@@ -107,30 +110,48 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 
-def make_workload(n: int, device, seed: int = 0):
-    import torch
+def host_workload(n: int, seed: int = 0):
+    """Clustered positions (numpy float32, (N, 3)) and the box size."""
     from jerald_gb300 import synth
     box = 100.0 * n / 64
-    pos = synth.clustered(n, box, seed=seed, device=device)
-    return pos.contiguous(), box
+    return np.ascontiguousarray(synth.clustered(n, box, seed=seed)), box
+
+
+def make_workload(n: int, device, seed: int = 0):
+    import torch
+    pos, box = host_workload(n, seed)
+    return torch.from_numpy(pos).to(device).contiguous(), box
+
+
+def noise_field(n: int):
+    from jerald_gb300 import synth
+    return synth.lognormal_noise((n, n, n), 0.1, seed=2)
 
 
 def make_target(pos, n, box, params, device, nstep: int = 2):
-    """The model's own output times lognormal noise (sigma 0.1); above 512^3
-    (where the plain primitive path would need several times the fused
-    step's memory) the noise field alone."""
+    """The model's own output (plain primitives, float32, no autograd) times
+    lognormal noise (sigma 0.1)."""
     import torch
-    from jerald_gb300 import synth
-    noise = torch.from_numpy(synth.lognormal_noise((n, n, n), 0.1, seed=2).astype(np.float32)).to(device)
-    if n > 512:
-        return noise.contiguous()
     from jerald_gb300.model import JERALDModel
     from jerald_gb300.pmesh import PMesh
     pm = PMesh(n, box, device=device, dtype=torch.float32)
     model = JERALDModel(pos, None, pm, Nstep=nstep, kind="sm")
     with torch.no_grad():
         F = model.evaluate(torch.as_tensor(params, dtype=torch.float32, device=device), pos, nstep)
-    return (F * noise).contiguous()
+    del model, pm
+    F *= torch.from_numpy(noise_field(n).astype(np.float32)).to(device)
+    torch.cuda.empty_cache()
+    return F.contiguous()
+
+
+def workload_config(n: int, nparts: int, box: float, nstep: int, recompute: bool = False, world: int = 1):
+    """The `config` object of both arms' lines."""
+    return {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, {nstep} sm layers + "
+                        f"ReLU map, L1 loss, fwd+adjoint ({5 * nstep + 3} grads)",
+            "nmesh": n, "nparts": int(nparts), "box": box, "nstep": nstep, "kind": "sm",
+            "memory_plan": "recompute force meshes" if recompute else "checkpoint",
+            "l2": "inputs larger than L2 (no flush)",
+            "parallelism": f"{world} replicas" if world > 1 else "single GPU"}
 
 
 def yardstick_bytes(N: int, nstep: int) -> int:
@@ -158,9 +179,23 @@ def time_primitives(pos, n, box, steps, warmup):
     sp = ct.c_void_p(st.cuda_stream)
     P = lambda t: ct.c_void_p(t.data_ptr())  # noqa: E731
     bp = b.ctypes.data_as(ct.c_void_p)
+    sws = torch.empty(int(_lib.load().jld_ppaint_box_sorted_workspace(N)), dtype=torch.uint8, device=pos.device)
+    keys = sws[:4 * N].view(torch.int32)
+    order = sws[(4 * N + 255) // 256 * 256:][:4 * N].view(torch.int32)
+    cws = torch.empty(int(_lib.load().jld_cell_sort_workspace(N)), dtype=torch.uint8, device=pos.device)
+    _lib.call("jld_cell_sort_f32", sp, P(pos), N, n, n, n, bp, P(keys), P(order), P(cws), cws.numel())
     ops = {
         "paint": (lambda: _lib.call("jld_ppaint_box_f32", sp, P(pos), N, None, ct.c_float(1.0), n, n, n, bp, P(mesh)),
                   12 * N + 4 * C),
+        # stable sort by cell key (keys and order written: 12N in, 8N out)
+        "cell_sort": (lambda: _lib.call("jld_cell_sort_f32", sp, P(pos), N, n, n, n, bp, P(keys), P(order), P(cws),
+                                        cws.numel()), 20 * N),
+        # paint from a kept cell-key order (the order read as well: 20N + 4C)
+        "paint_sorted_reuse": (lambda: _lib.call("jld_ppaint_sorted_f32", sp, P(pos), N, None, ct.c_float(1.0),
+                                                 n, n, n, bp, P(keys), P(order), P(mesh)), 20 * N + 4 * C),
+        # sort and sorted paint in one call (the paint's algorithmic bytes)
+        "paint_sorted": (lambda: _lib.call("jld_ppaint_box_sorted_f32", sp, P(pos), N, None, ct.c_float(1.0),
+                                           n, n, n, bp, P(mesh), P(sws), sws.numel()), 12 * N + 4 * C),
         "readout": (lambda: _lib.call("jld_preadout_box_f32", sp, P(pos), N, P(field), n, n, n, bp, -1, P(out)),
                     16 * N + 4 * C),
         "r2c": (lambda: _lib.call("jld_pfft_c_f32", sp, P(field), n, n, n, P(spec), P(ws), ws.numel()),
@@ -199,9 +234,11 @@ def _oracle_case(n_sample: int, threads: int):
     from jerald_gb300 import synth
     from oracle import fft as offt
     from oracle import cic as ocic
+    from oracle import ldl as oldl
     from oracle.ldl import LDLOracle
     offt.set_workers(threads)
     ocic.set_threads(threads)
+    oldl.set_threads(threads)
     box = 100.0 * n_sample / 64
     X = synth.clustered(n_sample, box, seed=0).astype(np.float64)
     p = synth.default_params(2)
@@ -217,7 +254,7 @@ def _oracle_line(n_sample: int, n_full: int, threads: int, dt: float, n_part_sam
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"oracle 2-layer fwd+grad at {n_sample}^3 ({n_part_sample} particles, "
                       f"{dt:.2f} s/step; CIC loops in C over {threads} particle ranges on {threads} threads, "
-                      f"FFT pocketfft with {threads} workers), "
+                      f"FFT pocketfft with {threads} workers, elementwise numpy on {threads} slabs), "
                       f"scaled by particle count to {n_full}^3"}
 
 
@@ -233,33 +270,46 @@ def cpu_baseline_sample(n_sample: int, n_full: int, steps: int = 1, threads: int
 
 
 def run_reference(args):
-    """The reference arm: the oracle port of the reference's CPU ops (the
-    reference itself needs MPI, FFTW and JAX, none of which exist here or
-    on the GPU machine) on all host threads, W untimed and K timed steps of a
-    128^3 sample of the workload, scaled by particle count."""
+    """The reference arm: the oracle's FP64 restatement of the reference's
+    CPU ops (the reference itself needs MPI, FFTW and JAX, none of which
+    exist on either host) on every host thread, on the full workload of this
+    benchmark: W untimed and K timed forward+gradient steps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    n_full = args.n
-    n_sample = max(16, min(128, n_full))
+    from jerald_gb300 import synth
+    from oracle import cic as ocic
+    from oracle import fft as offt
+    from oracle import ldl as oldl
     threads = os.cpu_count() or 1
-    step, npart = _oracle_case(n_sample, threads)
+    offt.set_workers(threads)
+    ocic.set_threads(threads)
+    oldl.set_threads(threads)
+    n, nstep = args.n, args.nstep
+    pos, box = host_workload(n, seed=0)
+    X = pos.astype(np.float64)
+    del pos
+    p = synth.default_params(nstep)
+    o = oldl.LDLOracle((n,) * 3, box, kind="sm", L1=True)
+    o.forward(p, X, np.zeros((n,) * 3), nstep)
+    tgt = o.cache["F"] * noise_field(n)
     for _ in range(args.warmup):
-        step()
-    dts = []
+        o.loss_and_grad(p, X, tgt, nstep)
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        step()
-        dts.append(time.perf_counter() - t0)
-    cb = _oracle_line(n_sample, n_full, threads, float(np.median(dts)), npart)
-    v = cb["value"]
+        loss, _ = o.loss_and_grad(p, X, tgt, nstep)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = 1.0 / dt
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"the full workload ({len(X)} particles, {n}^3 mesh): oracle FP64 fwd+grad, CIC loops in C "
+                    f"over {threads} particle ranges, FFT pocketfft with {threads} workers, elementwise numpy "
+                    f"on {threads} slabs"}
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": f"clustered {n_full}^3 particles+10% halos, {n_full}^3 mesh, 2 sm layers",
-                       "nmesh": n_full},
-            "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dt, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice + Gaussian halos)",
+            "impl": "reference", "config": workload_config(n, len(X), box, nstep), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "loss": loss}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -417,41 +467,74 @@ def run_loss_ext(args):
 
 
 def run_precision(args):
-    """Fused FP32 step vs the FP64 primitive pipeline (plain JERALDModel in
-    float64 on the same positions and target): loss and gradient errors."""
+    """Precision study on the benchmark workload: the fused FP32 step and the
+    plain FP32 primitives against the FP64 oracle (the CPU restatement of the
+    reference's pipeline) on the same positions and target; L1 loss in both
+    gradient conventions and L2 loss.  Prints one JSON object."""
     import torch
     import __graft_entry__
     __graft_entry__.build()
     from jerald_gb300 import synth
+    from jerald_gb300 import jaxpops_bind as jpo
     from jerald_gb300.ldl import FusedLDL
     from jerald_gb300.model import JERALDModel
     from jerald_gb300.pmesh import PMesh
+    from oracle import cic as ocic
+    from oracle import fft as offt
+    from oracle import ldl as oldl
+    threads = os.cpu_count() or 1
+    offt.set_workers(threads)
+    ocic.set_threads(threads)
+    oldl.set_threads(threads)
     dev = torch.device("cuda", 0)
-    n = args.n
-    params = synth.default_params(2)
-    pos, box = make_workload(n, dev, seed=0)
-    target = make_target(pos, n, box, params, dev)
-    res = {"precision": True, "n": n, "nparts": int(pos.shape[0])}
-    for mode in ("reference", "true"):
-        step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, grad_mode=mode, device=dev)
-        l32, g32 = step(pos, params, target)
-        l32, g32 = float(l32), g32.cpu().numpy()
-        del step
-        torch.cuda.empty_cache()
-        from jerald_gb300 import jaxpops_bind as jpo
-        jpo.set_fft_adjoint(mode)
-        pm = PMesh(n, box, device=dev, dtype=torch.float64)
-        model = JERALDModel(pos.double(), target.double(), pm, Nstep=2, kind="sm")
-        l64, g64 = model.loss_and_grad(torch.as_tensor(params, dtype=torch.float64))
-        jpo.set_fft_adjoint("reference")
-        l64, g64 = float(l64), g64.cpu().numpy()
-        del model, pm
-        torch.cuda.empty_cache()
-        rel = np.abs(g32 - g64) / np.abs(g64)
-        res[mode] = {"loss_f32": l32, "loss_f64": l64, "loss_rel_err": abs(l32 - l64) / abs(l64),
-                     "grad_rel_err_max": float(rel.max()), "grad_rel_err": rel.tolist(),
-                     "grad_norm_rel_err": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
-                     "grad_f64": g64.tolist()}
+    n, nstep = args.n, args.nstep
+    params = synth.default_params(nstep)
+    pos_h, box = host_workload(n, seed=0)
+    pos = torch.from_numpy(pos_h).to(dev)
+    target = make_target(pos, n, box, params, dev, nstep)
+    tgt_h = target.cpu().numpy().astype(np.float64)
+    X = pos_h.astype(np.float64)
+    ib = 5 * nstep + 2
+
+    def compare(g, g64):
+        g, g64 = np.asarray(g, np.float64), np.asarray(g64, np.float64)
+        rel = np.abs(g - g64) / np.abs(g64)
+        return {"grad_norm_rel_err": float(np.linalg.norm(g - g64) / np.linalg.norm(g64)),
+                "grad_rel_err": rel.tolist(),
+                "grad_rel_err_max_excl_b": float(np.delete(rel, ib).max()),
+                "grad_abs_err_b": float(abs(g[ib] - g64[ib]))}
+
+    res = {"precision": True, "n": n, "nparts": int(len(X)), "oracle_threads": threads}
+    for L1 in (True, False):
+        o = oldl.LDLOracle((n,) * 3, box, kind="sm", L1=L1)
+        t0 = time.perf_counter()
+        l64 = o.forward(params, X, tgt_h, nstep)
+        g64 = {m: o.backward(m) for m in ("reference", "true")}
+        t_oracle = time.perf_counter() - t0
+        F, diff = o.cache["F"], o.cache["diff"]
+        ties = int(np.count_nonzero(np.abs(diff) < 1e-5 * np.abs(F)))
+        key = "L1" if L1 else "L2"
+        res[key] = {"loss_f64": l64, "oracle_s": t_oracle, "grad_f64": {m: g.tolist() for m, g in g64.items()}}
+        if L1:
+            res[key]["near_tie_pixels"] = ties
+            res[key]["b_grad_tie_bound"] = 2.0 * ties / diff.size
+        del o
+        for mode in ("reference", "true"):
+            step = FusedLDL(n, box, pos.shape[0], nstep=nstep, kind="sm", L1=L1, grad_mode=mode, device=dev)
+            l32, g32 = step(pos, params, target)
+            l32, g32 = float(l32), g32.cpu().numpy()
+            del step
+            torch.cuda.empty_cache()
+            res[key][f"fused_{mode}"] = {"loss_rel_err": abs(l32 - l64) / abs(l64), **compare(g32, g64[mode])}
+        if L1:
+            pm = PMesh(n, box, device=dev, dtype=torch.float32)
+            model = JERALDModel(pos, target, pm, Nstep=nstep, kind="sm")
+            lp, gp = model.loss_and_grad(torch.as_tensor(params, dtype=torch.float32))
+            res[key]["plain_f32_reference"] = {"loss_rel_err": abs(float(lp) - l64) / abs(l64),
+                                               **compare(gp.cpu().numpy(), g64["reference"])}
+            del model, pm
+            torch.cuda.empty_cache()
+    jpo.set_fft_adjoint("reference")
     print(json.dumps(res), flush=True)
     return 0
 
@@ -612,12 +695,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Zel'dovich lattice + Gaussian halos)",
-                "config": {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, {nstep} sm layers + "
-                                       f"ReLU map, L1 loss, fwd+adjoint ({5 * nstep + 3} grads), graph-captured",
-                           "nmesh": n, "nparts": N, "box": box, "nstep": nstep, "kind": "sm",
-                           "memory_plan": "recompute force meshes" if args.recompute else "checkpoint",
-                           "l2": "inputs larger than L2 (no flush)", "parallelism": f"{world} replicas" if world > 1
-                           else "single GPU"},
+                "config": workload_config(n, N, box, nstep, args.recompute, world),
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,

@@ -124,6 +124,36 @@ JLD_API int jld_ppaint_box_method_f32(jld_stream_t stream, const float* pos, int
                               int32_t nx, int32_t ny, int32_t nz,
                               const float box[3], int32_t method, float* out);
 
+/* Sort by cell key (no counterpart in the reference, whose decomposition */
+/* computes the same key per particle, lib/parops_fast.h:91-93, but keeps  */
+/* input order).  Box-unit positions, the jaxpops_bind.py:161-164 prelude  */
+/* applied; keys[i] = the i-th smallest key, order[i] = its particle index, */
+/* ties in input order (numpy.argsort(keys, kind="stable")).  A stable LSD  */
+/* radix sort: workspace jld_cell_sort_workspace(nparts) bytes, 256-byte   */
+/* aligned; nparts < 2^31 - 1, Nx*Ny*Nz < 2^31.                            */
+JLD_API size_t jld_cell_sort_workspace(int64_t nparts);
+JLD_API int jld_cell_sort_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                              int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                              int32_t* keys, int32_t* order, void* ws, size_t ws_bytes);
+/* Paint of box-unit positions that walks a cell-key order from           */
+/* jld_cell_sort_f32 (replaces lpaint, lib/parops_fast.h:354-411, with the */
+/* same mesh): per run of equal keys (the particles of one cell) the eight */
+/* corner weights are summed first, in FP64 for runs of 16 or more         */
+/* particles, and added to `out` (zeroed first) once per corner.  The same */
+/* order serves repeated paints of the same positions, as the reference's  */
+/* stored layout does (useLayout, lib/parops_fast.h:484-531).              */
+JLD_API int jld_ppaint_sorted_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                                  const float* mass, float mass_scalar, int32_t nx, int32_t ny,
+                                  int32_t nz, const float box[3], const int32_t* keys,
+                                  const int32_t* order, float* out);
+/* jld_cell_sort_f32 then jld_ppaint_sorted_f32 in one call; workspace     */
+/* jld_ppaint_box_sorted_workspace(nparts) bytes, 256-byte aligned.        */
+JLD_API size_t jld_ppaint_box_sorted_workspace(int64_t nparts);
+JLD_API int jld_ppaint_box_sorted_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                                      const float* mass, float mass_scalar, int32_t nx, int32_t ny,
+                                      int32_t nz, const float box[3], float* out, void* ws,
+                                      size_t ws_bytes);
+
 /* Cell key of every particle: ((i % Nx) * Ny + j % Ny) * Nz + k % Nz with */
 /* i = int(p_x) etc., the per-particle key of the reference's             */
 /* decomposition (lib/parops_fast.h:91-93).  box == NULL: positions are in */

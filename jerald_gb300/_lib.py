@@ -72,6 +72,12 @@ _SIGS = {
     "jld_copy_from_host": [_c_void_p, _c_void_p, _c_void_p, _size, _i32],
     "jld_fft_pipe_status": [_c_void_p, _i32],
     "jld_wait_selftest": [_c_void_p, _i32, _c_void_p],
+    "jld_cell_sort_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _c_void_p, _c_void_p, _c_void_p,
+                          _size],
+    "jld_ppaint_sorted_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _f32, _i32, _i32, _i32, _c_void_p, _c_void_p,
+                              _c_void_p, _c_void_p],
+    "jld_ppaint_box_sorted_f32": [_c_void_p, _c_void_p, _i64, _c_void_p, _f32, _i32, _i32, _i32, _c_void_p,
+                                  _c_void_p, _c_void_p, _size],
 }
 _RESTYPES = {
     "jld_version": ct.c_char_p,
@@ -81,6 +87,8 @@ _RESTYPES = {
     "jld_fft_workspace_f64": _size,
     "jld_ldl_workspace_f32": _size,
     "jld_ldl_workspace_opt_f32": _size,
+    "jld_cell_sort_workspace": _size,
+    "jld_ppaint_box_sorted_workspace": _size,
 }
 _EXTRA_ARGS = {
     "jld_ldl_workspace_f32": [_i32, _i32, _i32, _i64, _i32],
@@ -88,6 +96,8 @@ _EXTRA_ARGS = {
     "jld_status_string": [ct.c_int],
     "jld_fft_workspace_f32": [_i32, _i32, _i32],
     "jld_fft_workspace_f64": [_i32, _i32, _i32],
+    "jld_cell_sort_workspace": [_i64],
+    "jld_ppaint_box_sorted_workspace": [_i64],
     "jld_version": [],
     "jld_last_error": [],
 }

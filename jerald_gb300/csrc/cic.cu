@@ -16,6 +16,7 @@
 // round-to-nearest intrinsics so they follow the reference's operation order.
 
 #include "common.cuh"
+#include "radix.cuh"
 
 namespace jld {
 
@@ -341,6 +342,132 @@ keys_kernel(PosSrc<T> src, int64_t n, Grid3 g, int32_t* __restrict__ keys) {
 }
 
 // ---------------------------------------------------------------------------
+// Sort by cell key, and the paint that walks that order.
+//
+// The key of a particle is the reference's decomposition key, int(p) % N per
+// axis flattened z fastest (lib/parops_fast.h:91-93), on positions that the
+// box prelude (jaxpops_bind.py:161-164) has put in [0, N]: every key lies in
+// [0, Nx*Ny*Nz).  radix.cuh sorts (key, particle index) pairs stably, so the
+// order equals numpy.argsort(keys, kind="stable").
+//
+// Sorted paint: the particles of one cell form a run of equal keys.  A
+// thread owns the runs that start in its chunk of kSortedChunk sorted slots
+// (a run that starts earlier belongs to an earlier chunk, however long it
+// is) and sums each run's eight corner weights: in FP32 for runs shorter
+// than kDenseRun particles, in FP64 for longer (dense-cell) runs, rounded
+// once to FP32.  Each run adds its lower-z face to the mesh; its upper-z face
+// is held back and added into the next run's lower-z face when that run is
+// the next cell of the same z row (the two faces are the same four cells),
+// else added to the mesh.  So a run costs four to eight atomics whatever its
+// length.  The corner cells of a run follow from its key; the per-particle
+// validity flags (the x mod L -> L edge, where int(p) = N) are applied to
+// each particle's weights, as in lpaint.
+constexpr int kSortedChunk = 8;
+constexpr int kDenseRun = 16;
+
+template <bool BOX>
+__global__ void __launch_bounds__(256)
+sort_keys_kernel(PosSrc<float> src, int64_t n, Grid3 g, uint32_t* __restrict__ keys, int32_t* __restrict__ order) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    float q[3];
+    load_pos<float, BOX>(src, p, q);
+    const int i = (int)q[0] % g.nx, j = (int)q[1] % g.ny, k = (int)q[2] % g.nz;
+    keys[p] = (uint32_t)(((int64_t)i * g.ny + j) * g.nz + k);
+    order[p] = (int32_t)p;
+  }
+}
+
+// Eight corner weights of one particle (index = bx | by << 1 | bz << 2),
+// each the lpaint product of the three axis weights, the mass and the
+// corner's validity flag; also the particle's corner offsets.
+template <bool BOX>
+__device__ __forceinline__ void particle_corners(const PosSrc<float>& src, int64_t p, const float* mass,
+                                                 float mscalar, const Grid3& g, float w[8], Corners<float>& c) {
+  float q[3];
+  load_pos<float, BOX>(src, p, q);
+  const float m = mass ? __ldg(mass + p) : mscalar;
+  cic_corners(q, g, c);
+  float lo[3], hi[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(1.f, c.d[a]); }
+#pragma unroll
+  for (int b = 0; b < 8; ++b) w[b] = mul_rn(mul_rn(corner_weight(lo, hi, b), m), corner_ok(c, b) ? 1.f : 0.f);
+}
+
+template <bool BOX>
+__global__ void __launch_bounds__(256)
+sorted_paint_kernel(PosSrc<float> src, const uint32_t* __restrict__ keys, const int32_t* __restrict__ order,
+                    int64_t n, const float* __restrict__ mass, float mscalar, Grid3 g, float* __restrict__ out) {
+  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * kSortedChunk; c0 < n;
+       c0 += nthr * kSortedChunk) {
+    const int64_t c1 = c0 + kSortedChunk < n ? c0 + kSortedChunk : n;
+    int64_t i = c0;
+    if (c0 > 0) {
+      const uint32_t before = __ldg(keys + c0 - 1);
+      while (i < c1 && __ldg(keys + i) == before) ++i;
+    }
+    double pend[4] = {0.0, 0.0, 0.0, 0.0};
+    uint32_t pend_off[4] = {0u, 0u, 0u, 0u};
+    uint32_t pend_key = 0u;
+    bool has_pend = false;
+    while (i < c1) {
+      const uint32_t key = __ldg(keys + i);
+      int64_t j = i + 1;
+      while (j < n && __ldg(keys + j) == key) ++j;
+      double sum[8];
+      Corners<float> c;
+      float w[8];
+      particle_corners<BOX>(src, __ldg(order + i), mass, mscalar, g, w, c);
+      if (j - i >= kDenseRun) {
+#pragma unroll
+        for (int b = 0; b < 8; ++b) sum[b] = (double)w[b];
+        for (int64_t t = i + 1; t < j; ++t) {
+          Corners<float> ct;
+          particle_corners<BOX>(src, __ldg(order + t), mass, mscalar, g, w, ct);
+#pragma unroll
+          for (int b = 0; b < 8; ++b) sum[b] = __dadd_rn(sum[b], (double)w[b]);
+        }
+      } else {
+        float sf[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) sf[b] = w[b];
+        for (int64_t t = i + 1; t < j; ++t) {
+          Corners<float> ct;
+          particle_corners<BOX>(src, __ldg(order + t), mass, mscalar, g, w, ct);
+#pragma unroll
+          for (int b = 0; b < 8; ++b) sf[b] = add_rn(sf[b], w[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < 8; ++b) sum[b] = (double)sf[b];
+      }
+      // the held-back upper-z face of the previous run is this run's lower-z
+      // face when this run is the next cell of the same z row
+      const bool chain = has_pend && key == pend_key + 1u && (key % (uint32_t)g.nz) != 0u;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        if (chain) {
+          sum[b] = __dadd_rn(sum[b], pend[b]);
+        } else if (has_pend && pend[b] != 0.0) {
+          atomicAdd(out + pend_off[b], (float)pend[b]);
+        }
+        if (sum[b] != 0.0) atomicAdd(out + corner_offset(c, b, g), (float)sum[b]);
+        pend[b] = sum[b + 4];
+        pend_off[b] = corner_offset(c, b + 4, g);
+      }
+      pend_key = key;
+      has_pend = true;
+      i = j;
+    }
+    if (has_pend) {
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (pend[b] != 0.0) atomicAdd(out + pend_off[b], (float)pend[b]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host side.
 
 template <typename T>
@@ -482,6 +609,54 @@ static int keys_impl(cudaStream_t st, const T* pos, int64_t nparts, int64_t nx, 
   return JLD_OK;
 }
 
+static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static size_t sorted_paint_ws(int64_t n) { return 2 * al256((size_t)n * 4) + radix_workspace(n); }
+
+static int key_bits_of(int64_t cells) {
+  int b = 1;
+  while (b < 31 && ((int64_t)1 << b) < cells) ++b;
+  return b;
+}
+
+static int cell_sort_impl(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny, int64_t nz,
+                          const float* box, int32_t* keys, int32_t* order, void* ws, size_t wsb, const char* who) {
+  int s = check_common<float>(pos, n, keys, nx, ny, nz, who);
+  if (s) return s;
+  if (!order) return set_error(JLD_ERR_ARG, "%s: order is NULL", who);
+  if (!box || !(box[0] > 0 && box[1] > 0 && box[2] > 0))
+    return set_error(JLD_ERR_ARG, "%s: box sizes must be positive", who);
+  if (n >= INT32_MAX) return set_error(JLD_ERR_UNSUPPORTED, "%s: at most 2^31 - 2 particles", who);
+  if (nx * ny * nz > INT32_MAX) return set_error(JLD_ERR_UNSUPPORTED, "%s: mesh too large for int32 keys", who);
+  if (n == 0) return JLD_OK;
+  if (n > 1 && (!ws || wsb < radix_workspace(n))) return set_error(JLD_ERR_WORKSPACE, "%s: workspace too small", who);
+  Grid3 g = make_grid(nx, ny, nz);
+  PosSrc<float> src = make_src<float>(pos, box, nx, ny, nz);
+  sort_keys_kernel<true><<<resident_grid(sort_keys_kernel<true>, n, 256), 256, 0, st>>>(src, n, g, (uint32_t*)keys,
+                                                                                       order);
+  JLD_LAUNCH_CHECK(who);
+  return radix_sort_pairs(st, (uint32_t*)keys, order, n, key_bits_of(g.cells()), ws, wsb, who);
+}
+
+static int sorted_paint_impl(cudaStream_t st, const float* pos, int64_t n, const float* mass, float ms, int64_t nx,
+                             int64_t ny, int64_t nz, const float* box, const int32_t* keys, const int32_t* order,
+                             float* out, const char* who) {
+  int s = check_common<float>(pos, n, out, nx, ny, nz, who);
+  if (s) return s;
+  if (!box || !(box[0] > 0 && box[1] > 0 && box[2] > 0))
+    return set_error(JLD_ERR_ARG, "%s: box sizes must be positive", who);
+  if (n > 0 && (!keys || !order)) return set_error(JLD_ERR_ARG, "%s: keys or order is NULL", who);
+  Grid3 g = make_grid(nx, ny, nz);
+  JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * g.cells(), st));
+  if (n == 0) return JLD_OK;
+  PosSrc<float> src = make_src<float>(pos, box, nx, ny, nz);
+  const int64_t chunks = (n + kSortedChunk - 1) / kSortedChunk;
+  sorted_paint_kernel<true><<<resident_grid(sorted_paint_kernel<true>, chunks, 256), 256, 0, st>>>(
+      src, (const uint32_t*)keys, order, n, mass, ms, g, out);
+  JLD_LAUNCH_CHECK(who);
+  return JLD_OK;
+}
+
 }  // namespace jld
 
 using namespace jld;
@@ -533,6 +708,37 @@ int jld_ppaint_box_method_f32(jld_stream_t s, const float* pos, int64_t n,
     return set_error(JLD_ERR_ARG, "jld_ppaint_box_method_f32: method must be 0 or 1");
   return paint_impl<float>(ST(s), pos, n, mass, ms, nx, ny, nz, box, method, out,
                            "jld_ppaint_box_method_f32");
+}
+
+size_t jld_cell_sort_workspace(int64_t nparts) { return nparts > 1 ? radix_workspace(nparts) : 0; }
+
+int jld_cell_sort_f32(jld_stream_t s, const float* pos, int64_t n, int32_t nx, int32_t ny, int32_t nz,
+                      const float box[3], int32_t* keys, int32_t* order, void* ws, size_t ws_bytes) {
+  clear_error();
+  return cell_sort_impl(ST(s), pos, n, nx, ny, nz, box, keys, order, ws, ws_bytes, "jld_cell_sort_f32");
+}
+
+int jld_ppaint_sorted_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass, float ms, int32_t nx,
+                          int32_t ny, int32_t nz, const float box[3], const int32_t* keys, const int32_t* order,
+                          float* out) {
+  clear_error();
+  return sorted_paint_impl(ST(s), pos, n, mass, ms, nx, ny, nz, box, keys, order, out, "jld_ppaint_sorted_f32");
+}
+
+size_t jld_ppaint_box_sorted_workspace(int64_t nparts) { return nparts > 0 ? sorted_paint_ws(nparts) : 0; }
+
+int jld_ppaint_box_sorted_f32(jld_stream_t s, const float* pos, int64_t n, const float* mass, float ms, int32_t nx,
+                              int32_t ny, int32_t nz, const float box[3], float* out, void* ws, size_t ws_bytes) {
+  clear_error();
+  const char* who = "jld_ppaint_box_sorted_f32";
+  if (n > 0 && (!ws || ws_bytes < sorted_paint_ws(n))) return set_error(JLD_ERR_WORKSPACE, "%s: workspace too small", who);
+  if (n == 0) return sorted_paint_impl(ST(s), pos, n, mass, ms, nx, ny, nz, box, nullptr, nullptr, out, who);
+  int32_t* keys = (int32_t*)ws;
+  int32_t* order = (int32_t*)((char*)ws + al256((size_t)n * 4));
+  void* rws = (char*)ws + 2 * al256((size_t)n * 4);
+  int st = cell_sort_impl(ST(s), pos, n, nx, ny, nz, box, keys, order, rws, ws_bytes - 2 * al256((size_t)n * 4), who);
+  if (st) return st;
+  return sorted_paint_impl(ST(s), pos, n, mass, ms, nx, ny, nz, box, keys, order, out, who);
 }
 
 int jld_preadout_f32(jld_stream_t s, const float* pos, int64_t n, const float* field,

@@ -41,24 +41,30 @@ def zeldovich(n: int, box: float, rms_cells: float = 0.5, seed: int = 0,
     """n^3 lattice particles plus a Zel'dovich displacement; returns (n^3, 3)."""
     if device is not None and str(device).startswith("cuda"):
         return _zeldovich_torch(n, box, rms_cells, seed, device, dtype)
+    import scipy.fft as sfft
     rng = np.random.default_rng(seed)
-    w = rng.standard_normal((n, n, n))
-    W = np.fft.rfftn(w)
+    W = sfft.rfftn(rng.standard_normal((n, n, n)), workers=-1)
     kx, ky, kz = _kgrid_np(n, box)
     k2 = kx ** 2 + ky ** 2 + kz ** 2
     kc = 0.5 * np.pi * n / box
     with np.errstate(divide="ignore", invalid="ignore"):
-        pk = np.where(k2 > 0, k2 ** (-1.25) * np.exp(-k2 / kc ** 2), 0.0)
-        delta = W * np.sqrt(pk)
-        inv = np.where(k2 > 0, 1.0 / k2, 0.0)
-    psi = [np.fft.irfftn(1j * kd * delta * inv, s=(n, n, n), axes=(0, 1, 2)) for kd in (kx, ky, kz)]
-    psi = np.stack([p.reshape(-1) for p in psi], axis=-1)
-    rms = np.sqrt(np.mean(np.sum(psi ** 2, axis=-1)))
+        # sqrt(P(k)) / k^2, zero at k = 0
+        W *= np.where(k2 > 0, np.sqrt(k2 ** (-1.25) * np.exp(-k2 / kc ** 2)) / k2, 0.0)
+    del k2
+    out = np.empty((n ** 3, 3), dtype=np.float64)
+    for d, kd in enumerate((kx, ky, kz)):
+        out[:, d] = sfft.irfftn(1j * kd * W, s=(n, n, n), axes=(0, 1, 2), workers=-1).reshape(-1)
+    del W
+    rms = np.sqrt(np.einsum("ij,ij->", out, out) / out.shape[0])
     cell = box / n
-    psi *= rms_cells * cell / rms
-    g = (np.arange(n) * cell)
-    q = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
-    return np.mod(q + psi, box).astype(dtype)
+    out *= rms_cells * cell / rms
+    g = np.arange(n) * cell
+    lat = out.reshape(n, n, n, 3)
+    lat[..., 0] += g[:, None, None]
+    lat[..., 1] += g[None, :, None]
+    lat[..., 2] += g[None, None, :]
+    np.mod(out, box, out=out)
+    return out.astype(dtype)
 
 
 def _zeldovich_torch(n, box, rms_cells, seed, device, dtype):

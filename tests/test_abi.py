@@ -98,3 +98,16 @@ def test_argument_errors_before_any_launch(libjld):
     ws.argtypes = [ct.c_void_p, ct.c_int32, ct.c_void_p]
     assert ws(None, 0, None) == 1 and b"polls" in libjld.jld_last_error()
     assert ws(None, (1 << 22) + 1, None) == 1
+    cs = libjld.jld_cell_sort_f32
+    cs.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
+                   ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_size_t]
+    assert cs(None, f, 10, 4, 4, 4, fbox, f, f, None, 0) == 3 and b"workspace" in libjld.jld_last_error()
+    assert cs(None, f, 10, 4, 4, 4, None, f, f, f, 1 << 20) == 1 and b"box" in libjld.jld_last_error()
+    assert cs(None, f, 10, 4, 4, 4, fbox, f, None, f, 1 << 20) == 1 and b"order" in libjld.jld_last_error()
+    libjld.jld_cell_sort_workspace.restype = ct.c_size_t
+    libjld.jld_cell_sort_workspace.argtypes = [ct.c_int64]
+    assert libjld.jld_cell_sort_workspace(1) == 0 and libjld.jld_cell_sort_workspace(5000) > 40000
+    bs = libjld.jld_ppaint_box_sorted_f32
+    bs.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_float, ct.c_int32, ct.c_int32,
+                   ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_size_t]
+    assert bs(None, f, 10, None, ct.c_float(1.0), 4, 4, 4, fbox, f, f, 16) == 3
