@@ -138,10 +138,11 @@ JLD_API int jld_cell_sort_f32(jld_stream_t stream, const float* pos, int64_t npa
 /* Paint of box-unit positions that walks a cell-key order from           */
 /* jld_cell_sort_f32 (replaces lpaint, lib/parops_fast.h:354-411, with the */
 /* same mesh): per run of equal keys (the particles of one cell) the eight */
-/* corner weights are summed first, in FP64 for runs of 16 or more         */
-/* particles, and added to `out` (zeroed first) once per corner.  The same */
-/* order serves repeated paints of the same positions, as the reference's  */
-/* stored layout does (useLayout, lib/parops_fast.h:484-531).              */
+/* corner weights are summed first -- runs longer than a warp's round of  */
+/* 32 in FP64, rounded once -- and added to `out` (zeroed first) once per  */
+/* corner.  The same order serves repeated paints of the same positions,  */
+/* as the reference's stored layout does (useLayout,                      */
+/* lib/parops_fast.h:484-531).                                             */
 JLD_API int jld_ppaint_sorted_f32(jld_stream_t stream, const float* pos, int64_t nparts,
                                   const float* mass, float mass_scalar, int32_t nx, int32_t ny,
                                   int32_t nz, const float box[3], const int32_t* keys,

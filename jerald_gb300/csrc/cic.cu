@@ -75,7 +75,21 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 #ifndef JLD_PAINT_MIN_CTAS
 #define JLD_PAINT_MIN_CTAS 6
 #endif
-template <typename T, bool BOX>
+// STAGED (float, 16-byte aligned positions and masses): each warp copies
+// the positions (and masses) of its batches two batches ahead into its own
+// shared-memory buffers with cp.async, so a batch's loads are in flight
+// while the warp paints the batch before it (ncu on the unstaged paint at
+// 256^3: long_scoreboard the top stall, DRAM at 21 % of peak).  A partial
+// last batch reads global memory directly.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+template <typename T, bool BOX, bool STAGED = false>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? JLD_PAINT_MIN_CTAS : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
              Grid3 g, T* __restrict__ out) {
@@ -88,14 +102,57 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
   // the lanes' own atomics would touch a dozen).
   __shared__ T wins[8][64];
   T* win = wins[threadIdx.x >> 5];
+  // per warp, two buffers of 32 positions (96 floats) and 32 masses
+  __shared__ __align__(16) float stage[STAGED ? 8 : 1][2][128];
+  float* stg = stage[STAGED ? (threadIdx.x >> 5) : 0][0];
   const int nax[3] = {g.nx, g.ny, g.nz};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+  const int64_t base0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
+  auto issue = [&](int64_t b, int buf) {
+    if (b + 32 <= n) {
+      float* d = stg + buf * 128;
+      if (lane < 24) cp_async16(d + 4 * lane, reinterpret_cast<const char*>(src.pos + 3 * b) + 16 * lane);
+      else if (mass) cp_async16(d + 96 + 4 * (lane - 24), reinterpret_cast<const char*>(mass + b) + 16 * (lane - 24));
+    }
+    cp_async_commit();
+  };
+  if constexpr (STAGED) {
+    issue(base0, 0);
+    issue(base0 + stride, 1);
+  }
+  int kb = 0;
+  for (int64_t base = base0; base < n; base += stride, ++kb) {
     const int64_t p = base + lane;
     const bool live = p < n;
     T q[3] = {T(0), T(0), T(0)};
     T m = T(0);
-    if (live) {
+    if constexpr (STAGED) {
+      cp_async_wait_1();
+      __syncwarp();
+      if (base + 32 <= n) {
+        const float* d = stg + (kb & 1) * 128;
+        const float x = d[3 * lane], y = d[3 * lane + 1], z = d[3 * lane + 2];
+        if (BOX) {
+          if (src.fast) {
+            q[0] = box_to_mesh_fast(x, src.box[0], src.inv[0]);
+            q[1] = box_to_mesh_fast(y, src.box[1], src.inv[1]);
+            q[2] = box_to_mesh_fast(z, src.box[2], src.inv[2]);
+          } else {
+            q[0] = box_to_mesh(x, src.box[0], src.cell[0]);
+            q[1] = box_to_mesh(y, src.box[1], src.cell[1]);
+            q[2] = box_to_mesh(z, src.box[2], src.cell[2]);
+          }
+        } else {
+          q[0] = x; q[1] = y; q[2] = z;
+        }
+        m = mass ? d[96 + lane] : mscalar;
+      } else if (live) {
+        load_pos<T, BOX>(src, p, q);
+        m = mass ? __ldg(mass + p) : mscalar;
+      }
+      __syncwarp();
+      issue(base + 2 * stride, kb & 1);
+    } else if (live) {
       load_pos<T, BOX>(src, p, q);
       m = mass ? __ldg(mass + p) : mscalar;
     }
@@ -350,20 +407,36 @@ keys_kernel(PosSrc<T> src, int64_t n, Grid3 g, int32_t* __restrict__ keys) {
 // [0, Nx*Ny*Nz).  radix.cuh sorts (key, particle index) pairs stably, so the
 // order equals numpy.argsort(keys, kind="stable").
 //
-// Sorted paint: the particles of one cell form a run of equal keys.  A
-// thread owns the runs that start in its chunk of kSortedChunk sorted slots
-// (a run that starts earlier belongs to an earlier chunk, however long it
-// is) and sums each run's eight corner weights: in FP32 for runs shorter
-// than kDenseRun particles, in FP64 for longer (dense-cell) runs, rounded
-// once to FP32.  Each run adds its lower-z face to the mesh; its upper-z face
-// is held back and added into the next run's lower-z face when that run is
+// Sorted paint: the particles of one cell form a run of equal keys.  A warp
+// walks kSortedSpan consecutive sorted slots in rounds of 32 (lane = slot):
+// each lane computes its particle's eight corner weights, a segmented
+// shuffle scan sums them per run within the round (runs are contiguous
+// lanes), and the lane that ends a run holds the run's sums.  A run that
+// reaches past the round's last lane stays open and its sums are carried to
+// the next round -- in FP64 once it holds kDenseRun particles, so a dense
+// cell (halo cores hold thousands of particles) is summed in FP64 and
+// rounded once, whatever its length; a run only splits where a warp's span
+// ends.  FP64 arithmetic runs only in rounds that continue such a run
+// (GB300 runs FP64 at a small fraction of its FP32 rate: a first version
+// that converted every run's sums to FP64 took 13 ms at 512^3).  Each
+// closed run adds its lower-z face to the mesh with one atomic per corner;
+// its upper-z face goes into the next run's lower-z face when that run is
 // the next cell of the same z row (the two faces are the same four cells),
-// else added to the mesh.  So a run costs four to eight atomics whatever its
-// length.  The corner cells of a run follow from its key; the per-particle
-// validity flags (the x mod L -> L edge, where int(p) = N) are applied to
-// each particle's weights, as in lpaint.
-constexpr int kSortedChunk = 8;
-constexpr int kDenseRun = 16;
+// else to the mesh.  For particles in cell order the end lanes of a round's
+// runs sit on consecutive cells, so its atomics touch a few 32-byte sectors
+// (a thread-per-chunk version, whose lanes' atomics lay 8 cells apart, took
+// 29 ms).  The corner cells of a run follow from any of its particles (all
+// particles of a cell share them); the per-particle validity flags (the
+// x mod L -> L edge, where int(p) = N) are applied to each particle's
+// weights, as in lpaint.
+constexpr int kSortedSpan = 32 * 64;
+constexpr int kDenseRun = 32;
+
+__device__ __forceinline__ unsigned lanemask_le() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+  return m;
+}
 
 template <bool BOX>
 __global__ void __launch_bounds__(256)
@@ -398,71 +471,186 @@ template <bool BOX>
 __global__ void __launch_bounds__(256)
 sorted_paint_kernel(PosSrc<float> src, const uint32_t* __restrict__ keys, const int32_t* __restrict__ order,
                     int64_t n, const float* __restrict__ mass, float mscalar, Grid3 g, float* __restrict__ out) {
-  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t c0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * kSortedChunk; c0 < n;
-       c0 += nthr * kSortedChunk) {
-    const int64_t c1 = c0 + kSortedChunk < n ? c0 + kSortedChunk : n;
-    int64_t i = c0;
-    if (c0 > 0) {
-      const uint32_t before = __ldg(keys + c0 - 1);
-      while (i < c1 && __ldg(keys + i) == before) ++i;
-    }
-    double pend[4] = {0.0, 0.0, 0.0, 0.0};
-    uint32_t pend_off[4] = {0u, 0u, 0u, 0u};
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned le = lanemask_le();
+  const uint32_t nz = (uint32_t)g.nz;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w0 = warp * kSortedSpan; w0 < n; w0 += nwarps * kSortedSpan) {
+    const int64_t w1 = w0 + kSortedSpan < n ? w0 + kSortedSpan : n;
+    // The open run carried from the previous round, the same in every lane:
+    // key, corner offsets, particle count, and sums -- FP32 (pend_f) while
+    // the run is shorter than kDenseRun particles, FP64 (pend_d) from then on.
+    bool has_pend = false, pend_dense = false;
     uint32_t pend_key = 0u;
-    bool has_pend = false;
-    while (i < c1) {
-      const uint32_t key = __ldg(keys + i);
-      int64_t j = i + 1;
-      while (j < n && __ldg(keys + j) == key) ++j;
-      double sum[8];
-      Corners<float> c;
+    int pend_cnt = 0;
+    float pend_f[8];
+    double pend_d[8];
+    uint32_t pend_off[8];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) { pend_f[b] = 0.f; pend_d[b] = 0.0; pend_off[b] = 0u; }
+    for (int64_t base = w0; base < w1; base += 32) {
+      const int64_t i = base + lane;
+      const bool live = i < w1;
+      const bool last_round = base + 32 >= w1;
+      const uint32_t key = live ? __ldg(keys + i) : 0xffffffffu;
       float w[8];
-      particle_corners<BOX>(src, __ldg(order + i), mass, mscalar, g, w, c);
-      if (j - i >= kDenseRun) {
+      uint32_t off[8];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) sum[b] = (double)w[b];
-        for (int64_t t = i + 1; t < j; ++t) {
-          Corners<float> ct;
-          particle_corners<BOX>(src, __ldg(order + t), mass, mscalar, g, w, ct);
+      for (int b = 0; b < 8; ++b) { w[b] = 0.f; off[b] = 0u; }
+      if (live) {
+        Corners<float> c;
+        particle_corners<BOX>(src, __ldg(order + i), mass, mscalar, g, w, c);
 #pragma unroll
-          for (int b = 0; b < 8; ++b) sum[b] = __dadd_rn(sum[b], (double)w[b]);
+        for (int b = 0; b < 8; ++b) off[b] = corner_offset(c, b, g);
+      }
+      const uint32_t kprev = __shfl_up_sync(full, key, 1);
+      const bool head = live && (lane == 0 ? !(has_pend && pend_key == key) : kprev != key);
+      const unsigned heads = __ballot_sync(full, head);
+      const unsigned lives = __ballot_sync(full, live);
+      const int last_live = 31 - __clz(lives);
+      const unsigned hb = heads & le;
+      const int sstart = hb ? 31 - __clz(hb) : -1;  // -1: this lane continues the open run
+      const int s0 = sstart < 0 ? 0 : sstart;
+      if (heads != lives) {  // some run covers more than one lane: segmented scan
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) {
+            const float t = __shfl_up_sync(full, w[b], o);
+            if (lane - o >= s0) w[b] = add_rn(w[b], t);
+          }
         }
+      }
+      const bool next_head = lane < 31 && ((heads >> (lane + 1)) & 1u);
+      const bool is_end = live && (lane == last_live || next_head);
+      const uint32_t kn = __shfl_down_sync(full, key, 1);
+      const bool chain_next = next_head && kn == key + 1u && (kn % nz) != 0u;
+      const bool lane0_head = heads & 1u;
+      const uint32_t key0 = __shfl_sync(full, key, 0);
+      // upper face of the run ending at each lane (read by the next run)
+      float up[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) up[b] = w[b + 4];
+      // 1. the open run closed before lane 0 (lane 0 starts another run):
+      //    lanes 0..7 flush it, its upper face into lane 0's run when that
+      //    is the next cell of the row
+      bool chain0 = false;
+      if (has_pend && lane0_head) {
+        chain0 = key0 == pend_key + 1u && (key0 % nz) != 0u;
+        float v = 0.f;
+        if (pend_dense) {
+#pragma unroll
+          for (int b = 0; b < 8; ++b)
+            if (lane == b) v = (float)pend_d[b];
+#pragma unroll
+          for (int b = 0; b < 4; ++b) pend_f[b + 4] = (float)pend_d[b + 4];
+        } else {
+#pragma unroll
+          for (int b = 0; b < 8; ++b)
+            if (lane == b) v = pend_f[b];
+        }
+        uint32_t o = pend_off[0];
+#pragma unroll
+        for (int b = 1; b < 8; ++b)
+          if (lane == b) o = pend_off[b];
+        if (lane < 8 && (lane < 4 || !chain0) && v != 0.f) atomicAdd(out + o, v);
+      }
+      // 2. lanes before the first head continue the open run, up to lane ce
+      const bool has_cont = has_pend && !lane0_head;
+      const unsigned before_head = heads ? ((1u << (__ffs(heads) - 1)) - 1u) : full;
+      const unsigned cont_lanes = lives & before_head;
+      const int ce = has_cont ? 31 - __clz(cont_lanes) : -1;
+      const bool cont_open = has_cont && ce == last_live && !last_round;
+      const int cnt_total = pend_cnt + ce + 1;
+      const bool cont_dense = has_cont && (pend_dense || cnt_total >= kDenseRun);
+      float cont_f[8];
+      double cont_d[8];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) { cont_f[b] = 0.f; cont_d[b] = 0.0; }
+      if (has_cont) {
+        float wc[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) wc[b] = __shfl_sync(full, w[b], ce);
+        if (cont_dense) {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) {
+            cont_d[b] = __dadd_rn(pend_dense ? pend_d[b] : (double)pend_f[b], (double)wc[b]);
+            cont_f[b] = (float)cont_d[b];
+          }
+        } else {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) cont_f[b] = add_rn(pend_f[b], wc[b]);
+        }
+        if (lane == ce) {
+#pragma unroll
+          for (int b = 0; b < 4; ++b) up[b] = cont_f[b + 4];
+        }
+        if (!cont_open) {  // the continued run closes at ce: lanes 0..7 flush it
+          const bool cn = __shfl_sync(full, chain_next ? 1 : 0, ce) != 0;
+          float v = 0.f;
+#pragma unroll
+          for (int b = 0; b < 8; ++b)
+            if (lane == b) v = cont_f[b];
+          uint32_t o = pend_off[0];
+#pragma unroll
+          for (int b = 1; b < 8; ++b)
+            if (lane == b) o = pend_off[b];
+          if (lane < 8 && (lane < 4 || !cn) && v != 0.f) atomicAdd(out + o, v);
+        }
+      }
+      // 3. runs that start in this round: lower face (plus the previous
+      //    run's upper face when chained), upper face unless chained onward
+      const int pl = sstart > 0 ? sstart - 1 : 0;
+      const uint32_t kp = __shfl_sync(full, key, pl);
+      float pu[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) pu[b] = __shfl_sync(full, up[b], pl);
+      if (sstart >= 0) {
+        const bool chain_prev = sstart > 0 ? (kp + 1u == key && (key % nz) != 0u) : chain0;
+        if (chain_prev) {
+#pragma unroll
+          for (int b = 0; b < 4; ++b) w[b] = add_rn(w[b], sstart > 0 ? pu[b] : pend_f[b + 4]);
+        }
+      }
+      const bool open = is_end && lane == last_live && !last_round && sstart >= 0;
+      if (is_end && sstart >= 0 && !open) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          if (w[b] != 0.f) atomicAdd(out + off[b], w[b]);
+        if (!chain_next) {
+#pragma unroll
+          for (int b = 4; b < 8; ++b)
+            if (w[b] != 0.f) atomicAdd(out + off[b], w[b]);
+        }
+      }
+      // 4. the run open at the round's end is carried
+      if (cont_open) {
+        pend_cnt = cnt_total;
+        if (cont_dense) {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) pend_d[b] = cont_d[b];
+        } else {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) pend_f[b] = cont_f[b];
+        }
+        pend_dense = cont_dense;
+        has_pend = true;
       } else {
-        float sf[8];
+        const bool any_open = __shfl_sync(full, open ? 1 : 0, last_live) != 0;
+        if (any_open) {
+          pend_key = __shfl_sync(full, key, last_live);
+          pend_cnt = last_live - __shfl_sync(full, sstart, last_live) + 1;
 #pragma unroll
-        for (int b = 0; b < 8; ++b) sf[b] = w[b];
-        for (int64_t t = i + 1; t < j; ++t) {
-          Corners<float> ct;
-          particle_corners<BOX>(src, __ldg(order + t), mass, mscalar, g, w, ct);
-#pragma unroll
-          for (int b = 0; b < 8; ++b) sf[b] = add_rn(sf[b], w[b]);
+          for (int b = 0; b < 8; ++b) {
+            pend_f[b] = __shfl_sync(full, w[b], last_live);
+            pend_off[b] = __shfl_sync(full, off[b], last_live);
+          }
+          pend_dense = false;
         }
-#pragma unroll
-        for (int b = 0; b < 8; ++b) sum[b] = (double)sf[b];
+        has_pend = any_open;
       }
-      // the held-back upper-z face of the previous run is this run's lower-z
-      // face when this run is the next cell of the same z row
-      const bool chain = has_pend && key == pend_key + 1u && (key % (uint32_t)g.nz) != 0u;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        if (chain) {
-          sum[b] = __dadd_rn(sum[b], pend[b]);
-        } else if (has_pend && pend[b] != 0.0) {
-          atomicAdd(out + pend_off[b], (float)pend[b]);
-        }
-        if (sum[b] != 0.0) atomicAdd(out + corner_offset(c, b, g), (float)sum[b]);
-        pend[b] = sum[b + 4];
-        pend_off[b] = corner_offset(c, b + 4, g);
-      }
-      pend_key = key;
-      has_pend = true;
-      i = j;
-    }
-    if (has_pend) {
-#pragma unroll
-      for (int b = 0; b < 4; ++b)
-        if (pend[b] != 0.0) atomicAdd(out + pend_off[b], (float)pend[b]);
     }
   }
 }
@@ -518,9 +706,20 @@ static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* ma
     if (box) paint_warpagg_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
     else paint_warpagg_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
   } else {
-    const unsigned grid = resident_grid(paint_kernel<T, true>, nparts, block);
-    if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
-    else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+    bool staged = false;
+    if constexpr (sizeof(T) == 4) {
+      staged = ((uintptr_t)pos & 15u) == 0 && ((uintptr_t)mass & 15u) == 0;
+      if (staged) {
+        const unsigned grid = resident_grid(paint_kernel<T, true, true>, nparts, block);
+        if (box) paint_kernel<T, true, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+        else paint_kernel<T, false, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+      }
+    }
+    if (!staged) {
+      const unsigned grid = resident_grid(paint_kernel<T, true>, nparts, block);
+      if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+      else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+    }
   }
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;
@@ -650,8 +849,8 @@ static int sorted_paint_impl(cudaStream_t st, const float* pos, int64_t n, const
   JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * g.cells(), st));
   if (n == 0) return JLD_OK;
   PosSrc<float> src = make_src<float>(pos, box, nx, ny, nz);
-  const int64_t chunks = (n + kSortedChunk - 1) / kSortedChunk;
-  sorted_paint_kernel<true><<<resident_grid(sorted_paint_kernel<true>, chunks, 256), 256, 0, st>>>(
+  const int64_t spans = (n + kSortedSpan - 1) / kSortedSpan;
+  sorted_paint_kernel<true><<<resident_grid(sorted_paint_kernel<true>, 32 * spans, 256), 256, 0, st>>>(
       src, (const uint32_t*)keys, order, n, mass, ms, g, out);
   JLD_LAUNCH_CHECK(who);
   return JLD_OK;

@@ -3,6 +3,8 @@
 // shared memory, persistent grid) of the strided and row passes.
 #pragma once
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <mutex>
 
@@ -82,9 +84,23 @@ inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, i
   // that fits alone.
   auto smem_of = [&](int c) { return (size_t)lines * c * 8 * (2 + nacc) + 64; };
   auto fits = [&](int c, size_t cap) { return c * lines / E <= 512 && h % c == 0 && smem_of(c) <= cap; };
+  // The narrowest tile taken at two CTAs per SM before a wider one at one
+  // CTA per SM: a tile reads `cols` consecutive complex values (8 * cols
+  // bytes) of each of its lines, every line in another part of the spectrum
+  // (4 MiB apart for the x pass at 1024^3).  At 1024 lines 64-byte pieces
+  // at one CTA per SM beat 32-byte pieces at two: the 1024^3 r2c took
+  // 8.58 instead of 12.28 ms; 512^3 and 256^3 (which get 8 or 16 columns at
+  // two CTAs anyway) did not change.  JLD_PIPE_MIN_COLS = 4, 8 or 16
+  // overrides the choice (a tuning knob; results are the same).
+  static const int min_cols_env = [] {
+    const char* e = getenv("JLD_PIPE_MIN_COLS");
+    const int v = e ? atoi(e) : 0;
+    return (v == 4 || v == 8 || v == 16) ? v : 0;
+  }();
+  const int min_cols = min_cols_env ? min_cols_env : (lines >= 1024 ? 8 : 4);
   int cols = 16;
-  while (cols >= 4 && !fits(cols, 112 * 1024)) cols >>= 1;
-  if (cols < 4) {
+  while (cols >= min_cols && !fits(cols, 112 * 1024)) cols >>= 1;
+  if (cols < min_cols) {
     cols = 16;
     while (cols >= 4 && !fits(cols, 226 * 1024)) cols >>= 1;
   }

@@ -220,8 +220,17 @@ class HostFeed:
         dev = step.device
         self.pos = [torch.empty((step.nparts, 3), dtype=torch.float32, device=dev) for _ in range(2)]
         self.tgt = [torch.empty(step.nmesh, dtype=torch.float32, device=dev) for _ in range(2)]
-        for t in self.pos + self.tgt:
-            t.zero_()
+        # capture_graph runs one eager step on these buffers first: spread
+        # positions, since particles piled into one cell would make that
+        # step's paint atomics contend (about 1 s at 1.5e8 particles)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(0)
+        box = torch.as_tensor(step.box, dtype=torch.float32, device=dev)
+        for t in self.pos:
+            torch.rand(t.shape, generator=gen, device=dev, out=t)
+            t.mul_(box)
+        for t in self.tgt:
+            t.fill_(1.0)
         self.mask = mask
         self.graphs = [step.capture_graph(self.pos[b], self.tgt[b], mask) for b in range(2)]
         self.copy = torch.cuda.Stream(dev)

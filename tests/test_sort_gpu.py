@@ -6,9 +6,9 @@ on: uniform and lattice-ordered clustered particles, every particle in one
 cell, the x mod L -> L edge, sizes that are not a multiple of the sort's
 4096-pair tiles, one particle.  The sorted paint must match the oracle's
 serial paint (the reference's lpaint, pinned in test_ref_pin.py) within 1e-5
-of the mesh scale, and its dense cells (runs of 16 or more particles, summed
-in FP64) the FP64 paint of the same float32 mesh positions within 1e-6
-relative.
+of the mesh scale, and its dense cells (runs carried over a warp's rounds,
+summed in FP64) the FP64 paint of the same float32 mesh positions within
+1e-6 relative.
 """
 import ctypes as ct
 
@@ -107,13 +107,14 @@ def test_sorted_paint_matches_oracle(jl, name, make, nm, box):
     got = out.cpu().numpy()
     scale = max(1.0, float(np.abs(ref).max()))
     assert np.abs(got - ref).max() <= 1e-5 * scale
-    # the same sort reused by the paint-only entry point gives the same mesh
+    # the paint-only entry point on a kept sort: the same mesh up to the
+    # order in which runs of one cell meet in the mesh's atomics
     _, _, dpos2, keys, order = _sort(jl, pos, nm, box)
     out2 = torch.empty_like(out)
     jl.call("jld_ppaint_sorted_f32", _st(), _p(dpos2), n, _p(dmass), ct.c_float(0.0), *nm,
             b.ctypes.data_as(ct.c_void_p), _p(keys), _p(order), _p(out2))
     torch.cuda.synchronize()
-    np.testing.assert_array_equal(out2.cpu().numpy(), got)
+    assert np.abs(out2.cpu().numpy() - got).max() <= 1e-6 * scale
 
 
 def test_sorted_paint_dense_cells_are_fp64_sums(jl):
