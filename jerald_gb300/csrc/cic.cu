@@ -15,6 +15,8 @@
 // Readouts gather the eight corners; weights and sums use explicit
 // round-to-nearest intrinsics so they follow the reference's operation order.
 
+#include <cstdlib>
+
 #include "common.cuh"
 #include "radix.cuh"
 
@@ -80,7 +82,8 @@ __device__ __forceinline__ T corner_weight(const T lo[3], const T hi[3], int bit
 // shared-memory buffers with cp.async, so a batch's loads are in flight
 // while the warp paints the batch before it (ncu on the unstaged paint at
 // 256^3: long_scoreboard the top stall, DRAM at 21 % of peak).  A partial
-// last batch reads global memory directly.
+// last batch reads global memory directly.  Measured slower than the
+// unstaged kernel at 512^3 (1.82 against 1.68 ms); kept selectable.
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
                "l"(gmem)
@@ -706,9 +709,16 @@ static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* ma
     if (box) paint_warpagg_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
     else paint_warpagg_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
   } else {
+    // The cp.async-staged kernel measured slower at 512^3 (paint primitive
+    // 1.82 against 1.68 ms, fused step 29.3 against 28.9 ms): the unstaged
+    // kernel is the default; JLD_PAINT_STAGED=1 selects the staged one.
+    static const bool use_staged = [] {
+      const char* e = getenv("JLD_PAINT_STAGED");
+      return e && e[0] == '1';
+    }();
     bool staged = false;
     if constexpr (sizeof(T) == 4) {
-      staged = ((uintptr_t)pos & 15u) == 0 && ((uintptr_t)mass & 15u) == 0;
+      staged = use_staged && ((uintptr_t)pos & 15u) == 0 && ((uintptr_t)mass & 15u) == 0;
       if (staged) {
         const unsigned grid = resident_grid(paint_kernel<T, true, true>, nparts, block);
         if (box) paint_kernel<T, true, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
