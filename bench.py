@@ -466,6 +466,44 @@ def run_loss_ext(args):
     return 0
 
 
+def run_hi(args):
+    """The fused step of the "HI" kind (star-map source in every layer,
+    depletion map) next to the "sm" step on the same workload: ms per step
+    of each, through captured graphs."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from jerald_gb300 import synth
+    from jerald_gb300.ldl import FusedLDL
+    dev = torch.device("cuda", 0)
+    n = args.n
+    pos, box = make_workload(n, dev)
+    target = make_target(pos, n, box, synth.default_params(2), dev)
+    sm = torch.from_numpy(synth.star_map(n, box, seed=5)).to(dev)
+    out = {"workload": f"clustered {n}^3, 2 layers, L1 loss; star map nonzero in 5 % of the cells", "nmesh": n}
+    for kind, params in (("sm", synth.default_params(2)), ("HI", synth.default_params_hi(2))):
+        step = FusedLDL(n, box, pos.shape[0], nstep=2, kind=kind, L1=True, device=dev,
+                        starmap=sm if kind == "HI" else None)
+        step(pos, params, target)
+        step.capture(pos, target)
+        for _ in range(args.warmup):
+            step.replay(params)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            step.replay(params)
+        e1.record(st)
+        torch.cuda.synchronize()
+        out[kind] = {"ms_per_step": e0.elapsed_time(e1) / args.steps, "loss": float(step.out[0]),
+                     "grad_norm": float(step.out[1:].norm()), "graph_kernels": step.graph_kernels(),
+                     "workspace_gb": step.workspace_bytes / 1e9}
+        del step
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_precision(args):
     """Precision study on the benchmark workload: the fused FP32 step and the
     plain FP32 primitives against the FP64 oracle (the CPU restatement of the
@@ -562,6 +600,8 @@ def main():
                     help="instead of the main workload: makemap of N synthetic gas particles (prints its own line)")
     ap.add_argument("--loss-ext", action="store_true",
                     help="instead of the main workload: the fused step with residual smoothing and a validation mask")
+    ap.add_argument("--hi", action="store_true",
+                    help="instead of the main workload: the fused HI-kind step next to the sm step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -577,6 +617,8 @@ def main():
         return run_snapmap(args)
     if args.loss_ext:
         return run_loss_ext(args)
+    if args.hi:
+        return run_hi(args)
 
     import torch
     from jerald_gb300 import replicas

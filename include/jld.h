@@ -354,6 +354,28 @@ JLD_API int jld_ldl_step_ext_f32(jld_stream_t stream, const float* pos, int64_t 
                                  int32_t options, const float* params, const float* target,
                                  const float* mask, const jld_ldl_loss_ext* ext, void* ws,
                                  size_t ws_bytes, double* out);
+/* The fused step for the "HI" kind (model.py:213-247 layers, 313-336      */
+/* final map): each layer's potential adds the star-map source,            */
+/*   potk = 1e-3 (a1 G1 r2c((rho+1e-8)^g1) + a2 G2 r2c(starmap^g2)),       */
+/* and the map is ReLU(w ReLU(rho + zs)^mu - D + b) with the depletion     */
+/* D = ReLU(beta1 c2r(r2c(starmap) Fk) + eta) + beta2 starmap^gamma3.      */
+/*   params  10 per layer (a1, g1, kh1, kl1, nu1, a2, g2, kh2, kl2, nu2),  */
+/*           then 12 (mu, w, b, beta1, khi, kli, nui, beta2, gamma3, xi,   */
+/*           eta, zs)                                                       */
+/*   starmap (nx, ny, nz) device float32 (starmap^e is taken as 0 where    */
+/*           starmap <= 0, as are its derivatives)                          */
+/* Other arguments and option bits as jld_ldl_step_f32.  The workspace    */
+/* (jld_ldl_workspace_hi_f32) is jld_ldl_workspace_opt_f32's plus          */
+/* nstep + 1 half spectra (8 (nz/2+1) nx ny bytes each) and two real       */
+/* meshes.  No counterpart in the reference, which evaluates the HI model  */
+/* through the primitives (jaxpops_bind) one operation at a time.          */
+JLD_API size_t jld_ldl_workspace_hi_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts,
+                                        int32_t nstep, int32_t options);
+JLD_API int jld_ldl_step_hi_f32(jld_stream_t stream, const float* pos, int64_t nparts,
+                                int32_t nx, int32_t ny, int32_t nz, const float box[3],
+                                int32_t nstep, int32_t L1, int32_t grad_mode, int32_t options,
+                                const float* params, const float* target, const float* mask,
+                                const float* starmap, void* ws, size_t ws_bytes, double* out);
 /* Device pointer to the step's error word in `ws` (0 = fine; nonzero = a  */
 /* pipelined pass gave up waiting for a tile copy and stopped early).      */
 JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz,

@@ -65,6 +65,8 @@ _SIGS = {
                          _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
     "jld_ldl_step_ext_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32,
                              _i32, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
+    "jld_ldl_step_hi_f32": [_c_void_p, _c_void_p, _i64, _i32, _i32, _i32, _c_void_p, _i32, _i32, _i32, _i32,
+                            _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _size, _c_void_p],
     "jld_ldl_positions_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _i32, _c_void_p],
     "jld_ldl_error_word_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
     "jld_ldl_order_f32": [_c_void_p, _i32, _i32, _i32, _i64, _i32, _c_void_p],
@@ -87,12 +89,14 @@ _RESTYPES = {
     "jld_fft_workspace_f64": _size,
     "jld_ldl_workspace_f32": _size,
     "jld_ldl_workspace_opt_f32": _size,
+    "jld_ldl_workspace_hi_f32": _size,
     "jld_cell_sort_workspace": _size,
     "jld_ppaint_box_sorted_workspace": _size,
 }
 _EXTRA_ARGS = {
     "jld_ldl_workspace_f32": [_i32, _i32, _i32, _i64, _i32],
     "jld_ldl_workspace_opt_f32": [_i32, _i32, _i32, _i64, _i32, _i32],
+    "jld_ldl_workspace_hi_f32": [_i32, _i32, _i32, _i64, _i32, _i32],
     "jld_status_string": [ct.c_int],
     "jld_fft_workspace_f32": [_i32, _i32, _i32],
     "jld_fft_workspace_f64": [_i32, _i32, _i32],

@@ -10,6 +10,7 @@
 #include "bins.cuh"
 #include "ldl_kernels.cuh"
 #include "ldl_pipe.cuh"
+#include "hi_kernels.cuh"
 #include "pipe_host.cuh"
 #include "zpipe.cuh"
 
@@ -19,7 +20,8 @@ struct LdlLayout {
   int64_t N, C, H;
   int nstep;
   size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
-      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, off_g4x, total;
+      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, off_g4x, off_s2, off_smu, off_dep, off_ctd,
+      total;
   TileGeom tg;
   int64_t part_doubles;
 };
@@ -46,7 +48,7 @@ static int g4_slots(int nstep, int options) {
 // Workspace layout.  Everything up to the error word is independent of the
 // options, then the binning buffers (kOptBinned), then the extra force-mesh
 // slots.
-static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep, int options) {
+static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep, int options, bool hi = false) {
   LdlLayout L;
   const int64_t h = nz / 2;
   L.N = N; L.nstep = nstep;
@@ -77,6 +79,14 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep, int op
     L.off_tiles = o; o += al(sizeof(int) * (3 * (size_t)L.tg.ntiles() + 1));
   }
   L.off_g4x = o; o += al(sizeof(float4) * L.C * (g4_slots(nstep, options) - 1));  // slots 1 ..
+  // HI kind: star-map spectrum per layer, pfft(star map), dep1, its cotangent
+  L.off_s2 = L.off_smu = L.off_dep = L.off_ctd = 0;
+  if (hi) {
+    L.off_s2 = o; o += al(sizeof(float2) * L.H * nstep);
+    L.off_smu = o; o += al(sizeof(float2) * L.H);
+    L.off_dep = o; o += al(sizeof(float) * L.C);
+    L.off_ctd = o; o += al(sizeof(float) * L.C);
+  }
   L.total = o;
   return L;
 }
@@ -89,7 +99,9 @@ struct StepArgs {
   bool use_pipe;         // TMA-pipelined strided passes where the mesh qualifies
   bool binned;           // particles binned into tiles; tile-privatized scatters
   int options;           // option bits (layout)
-  const float* params;   // device: 5*nstep (+3 for kind 0)
+  const float* params;   // device: npot*nstep (+3 for kind 0, +12 for kind 2)
+  int npot;              // parameters per layer: 5, or 10 for the HI kind
+  const float* starmap;  // HI kind: the star map (C floats), else nullptr
   const float* target; const float* mask;
   float n, index;        // loss smoothing exponent (0: none), map exponent (1: none)
   const float* field2;   // map factor or nullptr
@@ -130,8 +142,10 @@ static void launch_finish(cudaStream_t st, const double* part, int nblocks, int 
 
 static int ldl_step(const StepArgs& a) {
   const int nx = a.nx, ny = a.ny, nz = a.nz, h = nz / 2;
-  const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep, a.options);
+  const bool hi = a.kind == 2;
+  const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep, a.options, hi);
   const bool recompute = (a.options & kOptRecompute) != 0;
+  const int npot = a.npot;
   cudaStream_t st = a.st;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   JLD_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
@@ -292,15 +306,102 @@ static int ldl_step(const StepArgs& a) {
     return launch_line_pass<float>(st, pl.py, jn, none, sgn);
   };
 
+  // x FFT in place on buffer B (main + nyq), for the HI kind's star-map
+  // spectrum and its cotangent.
+  const PipeGeom pxs = pipe_geom(nx, ny, h, 0, 0);
+  auto xpass = [&](float2* B, int sgn) -> int {
+    LineJob<float> jm = job_x_internal<float>(pl, B, false), jn = job_x_internal<float>(pl, B + nyq_off, true),
+                   none;
+    if (!(pipe && pxs.ok)) return launch_line_pass<float>(st, pl.px, jm, jn, sgn);
+    CUtensorMap m;
+    int e = xmap(&m, B, pxs);
+    if (e) return e;
+    e = with_p2(nx, [&](auto sch) {
+      using Sch = decltype(sch);
+      auto kern = sgn < 0 ? spass_kernel<Sch, 0, -1> : spass_kernel<Sch, 0, 1>;
+      int r = ensure_smem(kern, pxs.smem);
+      if (r) return r;
+      kern<<<pxs.grid, pxs.nthr, pxs.smem, st>>>(m, B, pxs.g, pl.px.tw, err);
+      return 0;
+    });
+    if (e) return e;
+    JLD_LAUNCH_CHECK("spass_kernel");
+    return launch_line_pass<float>(st, pl.px, jn, none, sgn);
+  };
+  auto al16p = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+
+  // HI kind, layer l: S2 = FFT(sm^g2) in the internal layout (model.py:228).
+  auto star_spectrum = [&](int l, float2* S2) -> int {
+    const StarPow sp{a.params + npot * l};
+    int s2 = JLD_OK;
+    if (zr2c.ok && al16p(a.starmap)) {
+      s2 = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zr2c_pipe_kernel<Sch, StarPow>;
+        unsigned gz = 0;
+        int r = ensure_smem(kern, zr2c.smem);
+        if (!r) r = persistent_grid(kern, zr2c.nthr, zr2c.smem, zr2c.zt.ntiles, &gz);
+        if (r) return r;
+        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(a.starmap, sp, zr2c.zt, pl.twr, S2, pl.pz.tw, err);
+        return 0;
+      });
+      if (s2) return s2;
+      JLD_LAUNCH_CHECK("zr2c_pipe_kernel");
+    } else if ((s2 = launch_rfft_z_src<float, StarPow>(st, pl, a.starmap, sp, S2, S2 + nyq_off))) {
+      return s2;
+    }
+    if ((s2 = ypass(S2, -1))) return s2;
+    return xpass(S2, -1);
+  };
+
+  // HI kind, adjoint of layer l's star-map term from W (the cotangent
+  // spectrum of the potential): d a2, d kh2, d kl2, d nu2, then V2 =
+  // 1e-3 a2 G2 W / Nc back to real space (W[4]) and d g2.
+  const ZPipeGeom zc2r1 = a.use_pipe ? zpipe_geom(rows, h, 1, (size_t)(h + 1) * 8) : ZPipeGeom();
+  auto star_adjoint = [&](int l, const float* prm, float2* Wc, const float2* S2) -> int {
+    const unsigned g5 = (unsigned)std::min<int64_t>(
+        std::min<int64_t>(kMaxCellBlocks, L.part_doubles / 4), resident_grid(hi_src2_kernel, L.H, cblock));
+    hi_src2_kernel<<<g5, cblock, 0, st>>>(Wc, S2, nx, ny, nz, kt, prm, a.mode, scale, part);
+    JLD_LAUNCH_CHECK("hi_src2_kernel");
+    launch_finish(st, part, (int)g5, 4, 1, a.out, 1 + npot * l + 5, nullptr);
+    launch_finish(st, part + 1, (int)g5, 4, 3, a.out, 1 + npot * l + 7, nullptr);
+    int s2 = xpass(Wc, +1);
+    if (!s2) s2 = ypass(Wc, +1);
+    if (s2) return s2;
+    float* cts = (float*)W[4];
+    if (zc2r1.ok) {
+      s2 = with_p2(h, [&](auto sch) {
+        using Sch = decltype(sch);
+        auto kern = zc2r_pipe_kernel<Sch>;
+        unsigned gz = 0;
+        int r = ensure_smem(kern, zc2r1.smem);
+        if (!r) r = persistent_grid(kern, zc2r1.nthr, zc2r1.smem, zc2r1.zt.ntiles, &gz);
+        if (r) return r;
+        kern<<<gz, zc2r1.nthr, zc2r1.smem, st>>>(Wc, zc2r1.zt, pl.twr, cts, pl.pz.tw, err);
+        return 0;
+      });
+      if (s2) return s2;
+      JLD_LAUNCH_CHECK("zc2r_pipe_kernel");
+    } else if ((s2 = launch_irfft_z<float>(st, pl, Wc, Wc + nyq_off, cts))) {
+      return s2;
+    }
+    const unsigned g6 = (unsigned)std::min<int64_t>(kMaxCellBlocks, resident_grid(star_reduce_kernel, L.C, cblock));
+    star_reduce_kernel<<<g6, cblock, 0, st>>>(cts, a.starmap, prm, L.C, part);
+    JLD_LAUNCH_CHECK("star_reduce_kernel");
+    launch_finish(st, part, (int)g6, 1, 1, a.out, 1 + npot * l + 6, nullptr);
+    return JLD_OK;
+  };
+
   // Force mesh of layer l from its stored unit-mass density: source map and
   // r2c along z, y FFT, x FFT (S_l) with the filter and gradient factors,
   // inverse y of three channels, inverse z into the float4 mesh g4_l.
   auto force_mesh = [&](int l, float4* g4_l) -> int {
     int s = JLD_OK;
-    const float* prm = a.params + 5 * l;
+    const float* prm = a.params + npot * l;
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
     SourcePow src{prm, fact};
+    const float2* S2_l = hi ? (float2*)(ws + L.off_s2) + (size_t)L.H * l : nullptr;
     if (zr2c.ok) {
       s = with_p2(h, [&](auto sch) {
         using Sch = decltype(sch);
@@ -326,7 +427,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(xfilt_pipe_kernel<Sch>, px1.smem);
         if (r) return r;
         xfilt_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(mA, px1.g, kt, prm, a.kind, scale, S_l, W[1],
-                                                                    W[2], pl.px.tw, err);
+                                                                    W[2], pl.px.tw, err, S2_l);
         return 0;
       });
       if (s) return s;
@@ -337,7 +438,7 @@ static int ldl_step(const StepArgs& a) {
       int e = ensure_smem(xfilt_kernel<SC>, 2 * gx.smem1);
       if (e) return e;
       xfilt_kernel<SC><<<pipe ? gxn_tiles : (unsigned)gx.tiles, gx.nthr, 2 * gx.smem1, st>>>(
-          pl.px, pipe ? gxn : gx.sp, kt, prm, a.kind, scale, W[0], S_l, W[1], W[2]);
+          pl.px, pipe ? gxn : gx.sp, kt, prm, a.kind, scale, W[0], S_l, W[1], W[2], S2_l);
       return 0;
     });
     if (s) return s;
@@ -403,6 +504,7 @@ static int ldl_step(const StepArgs& a) {
   if ((s = paint_into(Xl(0), rho))) return s;
   for (int l = 0; l < a.nstep; ++l) {
     float4* g4_l = g4_of(l);
+    if (hi && (s = star_spectrum(l, (float2*)(ws + L.off_s2) + (size_t)L.H * l))) return s;
     if ((s = force_mesh(l, g4_l))) return s;
     update_kernel<<<resident_grid(update_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
     JLD_LAUNCH_CHECK("update_kernel");
@@ -413,13 +515,43 @@ static int ldl_step(const StepArgs& a) {
   float* rho_f = rho + (size_t)L.C * a.nstep;
   {
     const LossFields lf{rho_f, a.target, a.mask, a.field2, a.maskvalid};
-    const float* fprm = a.params + 5 * a.nstep;
-    const int nparam = 5 * a.nstep + (a.kind == 0 ? 3 : 0);
+    const float* fprm = a.params + npot * a.nstep;
+    const int nparam = npot * a.nstep + (a.kind == 0 ? 3 : (a.kind == 2 ? kHiFinalParams : 0));
     const int64_t max_blocks = std::min<int64_t>(kMaxCellBlocks, L.part_doubles / 5);
     // validation loss: reduced only with a validation mask, else 0
     double* lossv_out = a.lossv_slot ? a.out + 1 + nparam : nullptr;
     if (lossv_out && !a.maskvalid) JLD_CUDA_TRY(cudaMemsetAsync(lossv_out, 0, sizeof(double), st));
-    if (a.n > 0.f) {
+    if (hi) {
+      // dep1 = c2r(r2c(sm) Fk) (model.py:329-331), the map and loss, then
+      // d(khi, kli, nui, xi) from r2c(dL/d dep1)
+      const size_t wbytes = al(sizeof(float2) * L.H);
+      float2* smu = (float2*)(ws + L.off_smu);
+      float* dep = (float*)(ws + L.off_dep);
+      float* ctd = (float*)(ws + L.off_ctd);
+      if ((s = jld_pfft_c_f32((jld_stream_t)st, a.starmap, nx, ny, nz, smu, W[1], wbytes))) return s;
+      hi_dep_filter_kernel<<<resident_grid(hi_dep_filter_kernel, L.H, cblock), cblock, 0, st>>>(
+          W[0], smu, nx, ny, nz, kt, fprm, scale);
+      JLD_LAUNCH_CHECK("hi_dep_filter_kernel");
+      if ((s = jld_pifft_c_f32((jld_stream_t)st, W[0], nx, ny, nz, dep, W[1], wbytes))) return s;
+      const unsigned g7 = (unsigned)std::min<int64_t>(std::min<int64_t>(kMaxCellBlocks, L.part_doubles / 9),
+                                                      resident_grid(hi_loss_kernel, L.C, cblock));
+      hi_loss_kernel<<<g7, cblock, 0, st>>>(rho_f, a.starmap, dep, a.target, a.mask, L.C, fact, fprm, a.L1, npix,
+                                            rb, ctd, part);
+      JLD_LAUNCH_CHECK("hi_loss_kernel");
+      const int o = 1 + npot * a.nstep;
+      launch_finish(st, part, (int)g7, 9, 1, a.out, 0, npix);
+      launch_finish(st, part + 1, (int)g7, 9, 3, a.out, o, nullptr);       // mu, w, b
+      launch_finish(st, part + 4, (int)g7, 9, 1, a.out, o + 3, nullptr);   // beta1
+      launch_finish(st, part + 5, (int)g7, 9, 2, a.out, o + 7, nullptr);   // beta2, gamma3
+      launch_finish(st, part + 7, (int)g7, 9, 2, a.out, o + 10, nullptr);  // eta, zs
+      if ((s = jld_pfft_c_f32((jld_stream_t)st, ctd, nx, ny, nz, W[0], W[1], wbytes))) return s;
+      const unsigned g8 = (unsigned)std::min<int64_t>(std::min<int64_t>(kMaxCellBlocks, L.part_doubles / 4),
+                                                      resident_grid(hi_filter_grad_kernel, L.H, cblock));
+      hi_filter_grad_kernel<<<g8, cblock, 0, st>>>(W[0], smu, nx, ny, nz, kt, fprm, a.mode, scale, part);
+      JLD_LAUNCH_CHECK("hi_filter_grad_kernel");
+      launch_finish(st, part, (int)g8, 4, 3, a.out, o + 4, nullptr);      // khi, kli, nui
+      launch_finish(st, part + 3, (int)g8, 4, 1, a.out, o + 9, nullptr);  // xi
+    } else if (a.n > 0.f) {
       // diff -> c2r(r2c(diff) K) -> loss -> the same smoothing on its
       // cotangent (a real, even Fourier multiplier is its own adjoint)
       const size_t wbytes = al(sizeof(float2) * L.H);
@@ -465,9 +597,10 @@ static int ldl_step(const StepArgs& a) {
 
   // ---------------- adjoint layers
   for (int l = a.nstep - 1; l >= 0; --l) {
-    const float* prm = a.params + 5 * l;
+    const float* prm = a.params + npot * l;
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
+    float2* S2_l = hi ? (float2*)(ws + L.off_s2) + (size_t)L.H * l : nullptr;
     float4* g4_l = g4_of(l);
     // the last layer's mesh is still in its slot; layer 0's is not read
     if (recompute && l > 0 && l < a.nstep - 1 && (s = force_mesh(l, g4_l))) return s;
@@ -550,7 +683,8 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(xbwd_pipe_kernel<Sch>, px1.smem);
         if (r) return r;
         xbwd_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(m0, m1, m2, px1.g, kt, prm, a.kind, a.mode,
-                                                                   scale, W[1], part, pl.px.tw, err);
+                                                                   scale, W[1], part, pl.px.tw, err,
+                                                                   hi ? W[2] : nullptr);
         return 0;
       });
       if (s) return s;
@@ -564,15 +698,16 @@ static int ldl_step(const StepArgs& a) {
       if (e) return e;
       xbwd_kernel<SC><<<xb_grid, gx.nthr, 2 * gx.smem1, st>>>(pl.px, pipe ? gxn : gx.sp, kt, prm, a.kind, a.mode,
                                                                scale, W[0], W[3], S_l, W[1],
-                                                               part + (size_t)4 * nparts_x);
+                                                               part + (size_t)4 * nparts_x, hi ? W[2] : nullptr);
       return 0;
     });
     if (s) return s;
     JLD_LAUNCH_CHECK("xbwd_kernel");
     nparts_x += (int)xb_grid;
     // d alpha -> out[1+5l], d kh, d kl, d nu -> out[1+5l+2 .. 4]
-    launch_finish(st, part, nparts_x, 4, 1, a.out, 1 + 5 * l, nullptr);
-    launch_finish(st, part + 1, nparts_x, 4, 3, a.out, 1 + 5 * l + 2, nullptr);
+    launch_finish(st, part, nparts_x, 4, 1, a.out, 1 + npot * l, nullptr);
+    launch_finish(st, part + 1, nparts_x, 4, 3, a.out, 1 + npot * l + 2, nullptr);
+    if (hi && (s = star_adjoint(l, prm, W[2], S2_l))) return s;
     if ((s = ypass(W[1], +1))) return s;
     unsigned adj_blocks = zgrid;
     if (zadj.ok) {
@@ -598,7 +733,7 @@ static int ldl_step(const StepArgs& a) {
     }
     if (s) return s;
     JLD_LAUNCH_CHECK("zinv_adj_kernel");
-    launch_finish(st, part, (int)adj_blocks, 1, 1, a.out, 1 + 5 * l + 1, nullptr);
+    launch_finish(st, part, (int)adj_blocks, 1, 1, a.out, 1 + npot * l + 1, nullptr);
     if (l > 0 && !fuse_adj) {
       gather_vjp_kernel<<<resident_grid(gather_vjp_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, rb, Xb2, 1);
       JLD_LAUNCH_CHECK("gather_vjp_kernel");
@@ -651,10 +786,13 @@ JLD_API int jld_ldl_prepare_f32(int32_t nx, int32_t ny, int32_t nz, const float 
 static int step_entry(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny, int32_t nz,
                       const float box[3], int32_t nstep, int32_t kind, int32_t L1, int32_t grad_mode,
                       int32_t options, const float* params, const float* target, const float* mask,
-                      const jld_ldl_loss_ext* ext, void* ws, size_t ws_bytes, double* out, const char* who) {
+                      const jld_ldl_loss_ext* ext, const float* starmap, void* ws, size_t ws_bytes, double* out,
+                      const char* who) {
   int s = check_step_args(nx, ny, nz, nparts, nstep, box, who);
   if (s) return s;
-  if (kind != 0 && kind != 1) return set_error(JLD_ERR_ARG, "%s: kind must be 0 (sm) or 1 (dm)", who);
+  const bool hi = kind == 2;
+  if (kind != 0 && kind != 1 && !hi) return set_error(JLD_ERR_ARG, "%s: kind must be 0 (sm) or 1 (dm)", who);
+  if (hi && !starmap) return set_error(JLD_ERR_ARG, "%s: star map required", who);
   if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
   if (grad_mode != 0 && grad_mode != 1)
     return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
@@ -663,7 +801,7 @@ static int step_entry(jld_stream_t stream, const float* pos, int64_t nparts, int
     return set_error(JLD_ERR_UNSUPPORTED, "%s: binning needs fewer than 2^31 particles", who);
   const int paint_method = (options & kOptWarpPaint) ? 1 : 0;
   if (!pos || !params || !target || !out) return set_error(JLD_ERR_ARG, "%s: NULL pointer", who);
-  size_t need = ldl_layout(nx, ny, nz, nparts, nstep, options).total;
+  size_t need = ldl_layout(nx, ny, nz, nparts, nstep, options, hi).total;
   if (!ws || ws_bytes < need)
     return set_error(JLD_ERR_WORKSPACE, "%s: workspace of %zu bytes needed, got %zu", who, need,
                      ws ? ws_bytes : (size_t)0);
@@ -680,6 +818,8 @@ static int step_entry(jld_stream_t stream, const float* pos, int64_t nparts, int
   a.binned = (options & kOptBinned) != 0;
   a.options = options;
   a.params = params; a.target = target; a.mask = mask;
+  a.npot = hi ? kHiLayerParams : 5;
+  a.starmap = hi ? starmap : nullptr;
   a.n = ext ? ext->n : 0.f;
   a.index = ext ? ext->index : 1.f;
   a.field2 = ext ? ext->field2 : nullptr;
@@ -698,7 +838,7 @@ JLD_API int jld_ldl_step_f32(jld_stream_t stream, const float* pos, int64_t npar
                              double* out) {
   clear_error();
   return step_entry(stream, pos, nparts, nx, ny, nz, box, nstep, kind, L1, grad_mode, options, params, target,
-                    mask, nullptr, ws, ws_bytes, out, "jld_ldl_step_f32");
+                    mask, nullptr, nullptr, ws, ws_bytes, out, "jld_ldl_step_f32");
 }
 
 JLD_API int jld_ldl_step_ext_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
@@ -710,7 +850,22 @@ JLD_API int jld_ldl_step_ext_f32(jld_stream_t stream, const float* pos, int64_t 
   const char* who = "jld_ldl_step_ext_f32";
   if (!ext) return set_error(JLD_ERR_ARG, "%s: ext is NULL", who);
   return step_entry(stream, pos, nparts, nx, ny, nz, box, nstep, kind, L1, grad_mode, options, params, target,
-                    mask, ext, ws, ws_bytes, out, who);
+                    mask, ext, nullptr, ws, ws_bytes, out, who);
+}
+
+JLD_API size_t jld_ldl_workspace_hi_f32(int32_t nx, int32_t ny, int32_t nz, int64_t nparts, int32_t nstep,
+                                        int32_t options) {
+  if (nx < 1 || ny < 1 || nz < 2 || nparts < 1 || nstep < 1 || (options & ~kOptAll)) return 0;
+  return ldl_layout(nx, ny, nz, nparts, nstep, options, true).total;
+}
+
+JLD_API int jld_ldl_step_hi_f32(jld_stream_t stream, const float* pos, int64_t nparts, int32_t nx, int32_t ny,
+                                int32_t nz, const float box[3], int32_t nstep, int32_t L1, int32_t grad_mode,
+                                int32_t options, const float* params, const float* target, const float* mask,
+                                const float* starmap, void* ws, size_t ws_bytes, double* out) {
+  clear_error();
+  return step_entry(stream, pos, nparts, nx, ny, nz, box, nstep, 2, L1, grad_mode, options, params, target, mask,
+                    nullptr, starmap, ws, ws_bytes, out, "jld_ldl_step_hi_f32");
 }
 
 JLD_API int jld_ldl_error_word_f32(const void* ws, int32_t nx, int32_t ny, int32_t nz, int64_t nparts,

@@ -205,6 +205,21 @@ __device__ __forceinline__ void spec_columns(const SpecPass& sp, int ax, int64_t
   }
 }
 
+// Potential prefactor: 1e-2 (kinds sm, dm; model.py:159,198), 1e-3 for the
+// two-source HI kind (kind 2, model.py:232).
+__device__ __forceinline__ float pot_coef(int kind) { return kind == 2 ? 1e-3f : 1e-2f; }
+
+// HI kind: adds the star-map term 1e-3 a2 G2 S2 / Nc of the potential to p
+// (a2, kh2, kl2, nu2 at params[5], [7], [8], [9]; G2 = +exp(-k^2/kl2^2 -
+// kh2^2/k^2) k^nu2, the sm Green's function with the sign flipped).
+__device__ __forceinline__ void hi_add_src2(float2& p, float2 s2, const float* __restrict__ params, float scale,
+                                            float kx, float ky, float kz) {
+  const Green g2 = green_fn(kx, ky, kz, 0, __ldg(params + 7), __ldg(params + 8), __ldg(params + 9));
+  const float m = -1e-3f * __ldg(params + 5) * scale * g2.g;
+  p.x += s2.x * m;
+  p.y += s2.y * m;
+}
+
 // ---------------------------------------------------------------------------
 // Forward kernels.
 
@@ -233,7 +248,7 @@ template <int SCHED>
 __global__ void __launch_bounds__(512)
 xfilt_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict__ params,
              int kind, float scale, const float2* __restrict__ A, float2* __restrict__ S,
-             float2* __restrict__ T0, float2* __restrict__ T1) {
+             float2* __restrict__ T0, float2* __restrict__ T1, const float2* __restrict__ S2) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
@@ -251,13 +266,15 @@ xfilt_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restric
   __syncthreads();
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3),
               nu = __ldg(params + 4);
-  const float a = 1e-2f * alpha * scale;
+  const float a = pot_coef(kind) * alpha * scale;
   for (int f = tid; f < cols * n; f += nthr) {
     int c = f & (cols - 1), j = f >> sp.cshift;
     float2 v = s0[j * ld + c];
     Green gr = green_fn(__ldg(kt.kx + j), __ldg(kt.ky + ca[c]), __ldg(kt.kz + cb[c]), kind, kh, kl, nu);
     float m = a * gr.g;
     float2 p = make_float2(v.x * m, v.y * m);
+    if (S2 && colad[c] >= 0) hi_add_src2(p, S2[colad[c] + (int64_t)j * es], params, scale,
+                                         __ldg(kt.kx + j), __ldg(kt.ky + ca[c]), __ldg(kt.kz + cb[c]));
     s0[j * ld + c] = p;
     float cxv = __ldg(kt.cx + j);
     s1[j * ld + c] = make_float2(p.y * cxv, -p.x * cxv);  // -i c_x P
@@ -973,7 +990,8 @@ template <int SCHED>
 __global__ void __launch_bounds__(512)
 xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict__ params, int kind,
             int mode, float scale, const float2* __restrict__ Bx, const float2* __restrict__ D,
-            const float2* __restrict__ S, float2* __restrict__ Vout, double* __restrict__ partials) {
+            const float2* __restrict__ S, float2* __restrict__ Vout, double* __restrict__ partials,
+            float2* __restrict__ Wout) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int64_t colad[64];
   __shared__ int ca[64], cb[64];
@@ -991,7 +1009,8 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
   fft_tile<float, SCHED>(s1, ld, pl, sp.cshift, -1, tid, nthr);
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3),
               nu = __ldg(params + 4);
-  const float a1 = 1e-2f * scale;  // d P / d alpha = 1e-2 G S / Nc
+  const float pc = pot_coef(kind);
+  const float a1 = pc * scale;  // d P / d alpha = 1e-2 G S / Nc (1e-3 for HI)
   const int nz = 2 * sp.h, nyy = sp.ny;
   KahanF acc[4];
   for (int f = tid; f < cols * n; f += nthr) {
@@ -1005,6 +1024,7 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
       // W = i (c_x Bx + D)
       float2 q = make_float2(cx * bx.x + dd.x, cx * bx.y + dd.y);
       float2 W = make_float2(-q.y, q.x);
+      if (Wout) Wout[ad + (int64_t)j * es] = W;
       float2 Sv = S[ad + (int64_t)j * es];
       Green gr = green_fn(__ldg(kt.kx + j), __ldg(kt.ky + ca[c]), __ldg(kt.kz + kz), kind, kh, kl, nu);
       // Re(conj(W) S)
@@ -1013,11 +1033,11 @@ xbwd_kernel(LinePlan<float> pl, SpecPass sp, KTables kt, const float* __restrict
       float m_alpha = mode == 1 ? mk : 1.f;
       float m_green = mode == 1 ? mk : ((kz >= 1 && kz < nyy / 2) ? 2.f : 1.f);
       acc[0].add(m_alpha * a1 * gr.g * reWS);
-      float qg = m_green * 1e-2f * alpha * scale * reWS;
+      float qg = m_green * pc * alpha * scale * reWS;
       acc[1].add(qg * gr.dkh);
       acc[2].add(qg * gr.dkl);
       acc[3].add(qg * gr.dnu);
-      float vm = 1e-2f * alpha * scale * gr.g;
+      float vm = pc * alpha * scale * gr.g;
       v = make_float2(W.x * vm, W.y * vm);
     }
     s0[j * ld + c] = v;

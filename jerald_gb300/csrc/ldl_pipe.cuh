@@ -24,7 +24,8 @@ template <class Sch>
 __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, const float* __restrict__ params,
                   int kind, float scale, float2* __restrict__ S, float2* __restrict__ T0,
-                  float2* __restrict__ T1, const float2* __restrict__ tw, int* err) {
+                  float2* __restrict__ T1, const float2* __restrict__ tw, int* err,
+                  const float2* __restrict__ S2) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int cky[64], ckz[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -35,7 +36,7 @@ xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, c
   const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
   if (tid == 0 && ntl > 0) issue_tile<0>(&mA, s.slot[0], s.bar, g, blockIdx.x);
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3), nu = __ldg(params + 4);
-  const float a = 1e-2f * alpha * scale;
+  const float a = pot_coef(kind) * alpha * scale;
   ColWork wk{s.work, g.cols};
   ColWork ac{s.acc, g.cols};
   for (int i = 0; i < ntl; ++i) {
@@ -61,7 +62,10 @@ xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, c
       Green gr = green_fn(__ldg(kt.kx + j), __ldg(kt.ky + cky[c]), __ldg(kt.kz + ckz[c]), kind, kh, kl, nu);
       const float m = a * gr.g;
       float2 v = ac.at(c, j);
-      ac.at(c, j) = make_float2(v.x * m, v.y * m);
+      float2 p = make_float2(v.x * m, v.y * m);
+      if (S2) hi_add_src2(p, S2[base + c + (int64_t)j * g.es], params, scale, __ldg(kt.kx + j),
+                          __ldg(kt.ky + cky[c]), __ldg(kt.kz + ckz[c]));
+      ac.at(c, j) = p;
     }
     __syncthreads();
     auto inP = [&](int c, int j) { return ac.at(c, j); };
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant__ CUtensorMap mD,
                  const __grid_constant__ CUtensorMap mS, SGeom g, KTables kt, const float* __restrict__ params,
                  int kind, int mode, float scale, float2* __restrict__ Vout, double* __restrict__ partials,
-                 const float2* __restrict__ tw, int* err) {
+                 const float2* __restrict__ tw, int* err, float2* __restrict__ Wout) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int cky[64], ckz[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -206,8 +210,9 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
   const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
   if (tid == 0 && ntl > 0) issue_tile<0>(&mBx, s.slot[0], s.bar, g, blockIdx.x);
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3), nu = __ldg(params + 4);
-  const float a1 = 1e-2f * scale;
-  const float vm0 = 1e-2f * alpha * scale;
+  const float pc = pot_coef(kind);
+  const float a1 = pc * scale;
+  const float vm0 = pc * alpha * scale;
   const int nz = 2 * g.h;
   ColWork wk{s.work, g.cols};
   ColWork ac{s.acc, g.cols};
@@ -246,6 +251,7 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
       const int c = f & (g.cols - 1), j = f >> g.cshift;
       const int kz = ckz[c];
       const float2 W = ac.at(c, j);
+      if (Wout) Wout[base + c + (int64_t)j * g.es] = W;
       const float2 Sv = slot[j * g.cols + c];
       Green gr = green_fn(__ldg(kt.kx + j), __ldg(kt.ky + cky[c]), __ldg(kt.kz + kz), kind, kh, kl, nu);
       const float reWS = W.x * Sv.x + W.y * Sv.y;
@@ -253,7 +259,7 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
       const float m_alpha = mode == 1 ? mk : 1.f;
       const float m_green = mode == 1 ? mk : ((kz >= 1 && kz < g.ny / 2) ? 2.f : 1.f);
       acc[0].add(m_alpha * a1 * gr.g * reWS);
-      const float qg = m_green * 1e-2f * alpha * scale * reWS;
+      const float qg = m_green * pc * alpha * scale * reWS;
       acc[1].add(qg * gr.dkh);
       acc[2].add(qg * gr.dkl);
       acc[3].add(qg * gr.dnu);

@@ -1,7 +1,7 @@
 """Fused LDL forward + adjoint step (libjld's jld_ldl_step_f32) with CUDA-graph
 capture.
 
-One call evaluates the loss of model.py (kinds "sm" and "dm") and its
+One call evaluates the loss of model.py (kinds "sm", "dm" and "HI") and its
 gradient with respect to every parameter, the way
 JERALDModel.loss_and_grad does through the primitives, but with the
 elementwise source, filter and gradient kernels fused into the FFT passes,
@@ -22,7 +22,7 @@ import torch
 
 from . import _lib
 
-_KINDS = {"sm": 0, "dm": 1}
+_KINDS = {"sm": 0, "dm": 1, "HI": 2}
 _MODES = {"reference": 0, "true": 1}
 _PAINT = {"atomic": 0, "warp": 1, "tiled": 4}
 
@@ -54,13 +54,26 @@ def _finish_capture(g) -> None:
 class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
                  grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
-                 pipelined: bool = True, recompute: bool = False, n: float = 0.0, index: float = 1.0):
+                 pipelined: bool = True, recompute: bool = False, n: float = 0.0, index: float = 1.0,
+                 starmap=None):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
         self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
         if kind not in _KINDS:
-            raise ValueError("kind must be 'sm' or 'dm' for the fused step (use JERALDModel for 'HI')")
+            raise ValueError("kind must be 'sm', 'dm' or 'HI'")
         self.kind = kind
+        # HI kind (model.py:213-247, 313-336): the star map is a fixed input
+        # of the model, a float32 mesh kept on the device
+        self.starmap = None
+        if kind == "HI":
+            if starmap is None:
+                raise ValueError("Star map required for HI target")
+            if n != 0 or index != 1:
+                raise ValueError("the fused HI step has no residual smoothing or map exponent")
+            sm = torch.as_tensor(starmap, dtype=torch.float32, device=device).contiguous()
+            if sm.numel() != int(np.prod(self.nmesh)):
+                raise ValueError("starmap must be a mesh of the step's shape")
+            self.starmap = sm
         self.L1 = (kind != "dm") if L1 is None else bool(L1)
         self.grad_mode = grad_mode
         self.paint_method = paint_method
@@ -68,10 +81,11 @@ class FusedLDL:
         self.recompute = bool(recompute)
         self.nparts = int(nparts)
         self.nstep = int(nstep)
-        self.nparams = 5 * self.nstep + (3 if kind == "sm" else 0)
+        self.nparams = {"sm": 5 * self.nstep + 3, "dm": 5 * self.nstep, "HI": 10 * self.nstep + 12}[kind]
         self.device = torch.device(device)
         lib = _lib.load()
-        nbytes = lib.jld_ldl_workspace_opt_f32(*self.nmesh, self.nparts, self.nstep, self.options)
+        ws_fn = lib.jld_ldl_workspace_hi_f32 if kind == "HI" else lib.jld_ldl_workspace_opt_f32
+        nbytes = ws_fn(*self.nmesh, self.nparts, self.nstep, self.options)
         if nbytes == 0:
             raise ValueError("invalid fused-step geometry")
         self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
@@ -107,8 +121,17 @@ class FusedLDL:
             if m is not None and (m.dtype != torch.float32 or not m.is_contiguous() or m.numel() != C):
                 raise ValueError(f"{name} must be a contiguous float32 mesh")
         ptr = lambda t: ct.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
-        ext = _LossExt(self.n, self.index, ptr(field2), ptr(maskvalid))
         st = ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        if self.kind == "HI":
+            if field2 is not None or maskvalid is not None:
+                raise ValueError("the fused HI step takes no field2 or validation mask")
+            _lib.call("jld_ldl_step_hi_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
+                      self.box.ctypes.data_as(ct.c_void_p), self.nstep, int(self.L1), _MODES[self.grad_mode],
+                      self.options, ct.c_void_p(self.params.data_ptr()), ct.c_void_p(target.data_ptr()),
+                      ptr(mask), ct.c_void_p(self.starmap.data_ptr()), ct.c_void_p(self.ws.data_ptr()),
+                      self.ws.numel(), ct.c_void_p(self._buf.data_ptr()))
+            return
+        ext = _LossExt(self.n, self.index, ptr(field2), ptr(maskvalid))
         _lib.call("jld_ldl_step_ext_f32", st, ct.c_void_p(pos.data_ptr()), self.nparts, *self.nmesh,
                   self.box.ctypes.data_as(ct.c_void_p), self.nstep, _KINDS[self.kind], int(self.L1),
                   _MODES[self.grad_mode], self.options,

@@ -14,6 +14,12 @@ seed, with the shapes and distributions of the workload definitions:
   (0.05, 1.0, 0.5, 2.0, 1.0), then (mu, w, b) = (1.5, 1.0, -0.1).  In the
   model's filter exp(-k^2/kl^2 - kh^2/k^2) these kh, kl give
   exp(-(k/2)^2) exp(-(0.5/k)^2).
+* default_params_hi(nstep): the "HI" kind's per layer (a1, g1, kh1, kl1,
+  nu1, a2, g2, kh2, kl2, nu2) = (0.5, 1.0, 0.5, 2.0, 1.0, 0.3, 0.8, 0.6,
+  1.5, 0.5), then (mu, w, b, beta1, khi, kli, nui, beta2, gamma3, xi, eta,
+  zs) = (1.2, 1.0, 0.2, 0.3, 0.5, 2.0, 0.5, 0.1, 0.9, 0.05, 0.1, 0.5).
+* star_map(n, box, seed, frac): a stellar-mass mesh, zero outside the
+  densest `frac` of the cells of a smoothed lognormal field.
 
 Generation runs in numpy (CPU, float64) or in torch on a CUDA device (for the
 large workloads); the two draw different random streams.
@@ -28,6 +34,33 @@ FINAL_DEFAULT = (1.5, 1.0, -0.1)
 
 def default_params(nstep: int = 2) -> np.ndarray:
     return np.array(list(LAYER_DEFAULT) * nstep + list(FINAL_DEFAULT), dtype=np.float64)
+
+
+HI_LAYER_DEFAULT = (0.5, 1.0, 0.5, 2.0, 1.0, 0.3, 0.8, 0.6, 1.5, 0.5)
+HI_FINAL_DEFAULT = (1.2, 1.0, 0.2, 0.3, 0.5, 2.0, 0.5, 0.1, 0.9, 0.05, 0.1, 0.5)
+
+
+def default_params_hi(nstep: int = 2) -> np.ndarray:
+    return np.array(list(HI_LAYER_DEFAULT) * nstep + list(HI_FINAL_DEFAULT), dtype=np.float64)
+
+
+def star_map(n: int, box: float, seed: int = 0, frac: float = 0.05) -> np.ndarray:
+    """(n, n, n) float32 stellar-mass mesh: exp(2 g) of a Gaussian field g
+    smoothed on two cells, kept in the densest `frac` of the cells and zero
+    elsewhere, scaled to mean 1 over the cells it keeps."""
+    import scipy.fft as sfft
+    rng = np.random.default_rng(seed)
+    W = sfft.rfftn(rng.standard_normal((n, n, n)), workers=-1)
+    kx, ky, kz = _kgrid_np(n, box)
+    r = 2.0 * box / n
+    W *= np.exp(-0.5 * (kx ** 2 + ky ** 2 + kz ** 2) * r * r)
+    g = sfft.irfftn(W, s=(n, n, n), workers=-1)
+    g /= g.std()
+    f = np.exp(2.0 * g)
+    cut = np.quantile(f, 1.0 - frac)
+    out = np.where(f > cut, f, 0.0)
+    out /= out[out > 0].mean()
+    return out.astype(np.float32)
 
 
 def _kgrid_np(n: int, box: float):

@@ -111,3 +111,17 @@ def test_argument_errors_before_any_launch(libjld):
     bs.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_float, ct.c_int32, ct.c_int32,
                    ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_size_t]
     assert bs(None, f, 10, None, ct.c_float(1.0), 4, 4, 4, fbox, f, f, 16) == 3
+    hi = libjld.jld_ldl_step_hi_f32
+    hi.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int64, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p,
+                   ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                   ct.c_void_p, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+    assert hi(None, f, 8, 4, 4, 4, fbox, 2, 1, 0, 0, f, f, None, None, f, 1 << 30, f) == 1
+    assert b"star map" in libjld.jld_last_error()
+    for fn in (libjld.jld_ldl_workspace_hi_f32, libjld.jld_ldl_workspace_opt_f32):
+        fn.restype = ct.c_size_t
+        fn.argtypes = [ct.c_int32] * 3 + [ct.c_int64, ct.c_int32, ct.c_int32]
+    # the HI workspace adds nstep + 1 half spectra and two real meshes
+    extra = libjld.jld_ldl_workspace_hi_f32(32, 32, 32, 1000, 2, 0) - \
+        libjld.jld_ldl_workspace_opt_f32(32, 32, 32, 1000, 2, 0)
+    assert extra == 3 * 8 * 32 * 32 * 17 + 2 * 4 * 32 ** 3
+    assert hi(None, f, 8, 4, 4, 4, fbox, 2, 1, 0, 0, f, f, None, f, f, 16, f) == 3

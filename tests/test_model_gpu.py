@@ -96,13 +96,6 @@ def test_losstest_replica_f64():
     assert _rel(g.cpu().numpy(), g_o).max() < 1e-7
 
 
-def _hi_params(nstep):
-    # per layer (alpha1, gamma1, kh1, kl1, nu1, alpha2, gamma2, kh2, kl2, nu2),
-    # then (mu, w, b, beta1, khi, kli, nui, beta2, gamma3, xi, eta, zs)
-    layer = [0.5, 1.0, 0.5, 2.0, 1.0, 0.3, 0.8, 0.6, 1.5, 0.5]
-    final = [1.2, 1.0, 0.2, 0.3, 0.5, 2.0, 0.5, 0.1, 0.9, 0.05, 0.1, 0.5]
-    return np.array(layer * nstep + final, dtype=np.float64)
-
 
 @pytest.mark.parametrize("case", ["HI", "sm_smooth", "sm_index_field2_valid"])
 def test_plain_model_options_match_oracle_and_differences(case):
@@ -123,7 +116,7 @@ def test_plain_model_options_match_oracle_and_differences(case):
     kw = dict(L1=False)
     opts = {}
     if case == "HI":
-        kind, p = "HI", _hi_params(2)
+        kind, p = "HI", synth.default_params_hi(2)
         opts["starmap"] = np.exp(0.3 * rng.standard_normal((n,) * 3))
     elif case == "sm_smooth":
         kind, p = "sm", synth.default_params(2)
