@@ -499,7 +499,29 @@ def run_hi(args):
         out[kind] = {"ms_per_step": e0.elapsed_time(e1) / args.steps, "loss": float(step.out[0]),
                      "grad_norm": float(step.out[1:].norm()), "graph_kernels": step.graph_kernels(),
                      "workspace_gb": step.workspace_bytes / 1e9}
-        del step
+        if kind == "HI" and not args.no_plain:
+            # the plain FP32 primitives one by one (JERALDModel, torch autograd)
+            from jerald_gb300.model import JERALDModel
+            from jerald_gb300.pmesh import PMesh
+            grad = step.out[1:].cpu().numpy()
+            del step
+            pm = PMesh(n, box, device=dev, dtype=torch.float32)
+            model = JERALDModel(pos, target, pm, Nstep=2, kind="HI", L1=True, starmap=sm)
+            pt = torch.as_tensor(params, dtype=torch.float32)
+            model.loss_and_grad(pt)
+            torch.cuda.synchronize()
+            e0.record(st)
+            for _ in range(3):
+                lp, gp = model.loss_and_grad(pt)
+            e1.record(st)
+            torch.cuda.synchronize()
+            gp = gp.cpu().numpy()
+            out[kind]["plain_ms_per_step"] = e0.elapsed_time(e1) / 3
+            out[kind]["speedup_vs_plain"] = out[kind]["plain_ms_per_step"] / out[kind]["ms_per_step"]
+            out[kind]["grad_rel_diff_vs_plain_f32"] = float(np.linalg.norm(grad - gp) / np.linalg.norm(gp))
+            del model, pm
+        else:
+            del step
     print(json.dumps(out), flush=True)
     return 0
 

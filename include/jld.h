@@ -67,9 +67,9 @@ JLD_API const char* jld_status_string(int status);
 JLD_API const char* jld_last_error(void);
 /* Copies `bytes` from page-locked host memory to device memory with a  */
 /* kernel that reads the host buffer directly (over NVLink-C2C on a GB300 */
-/* node) instead of the copy engines; `ctas` CTAs of 512 threads (<= 0:   */
-/* two per SM).  Both pointers 16-byte aligned.  Stream-ordered.  No      */
-/* counterpart in the reference (host-feed helper).                       */
+/* node) instead of the copy engines; `ctas` CTAs of 1024 threads (<= 0: */
+/* four), each holding an SM.  Both pointers 16-byte aligned.             */
+/* Stream-ordered.  No counterpart in the reference (host-feed helper).   */
 JLD_API int jld_copy_from_host(jld_stream_t stream, void* dst, const void* src_host, size_t bytes,
                                int32_t ctas);
 /* Number of kernel nodes in a captured CUDA graph (cudaGraph_t passed as */
@@ -302,6 +302,11 @@ JLD_API int jld_pfft_c_static_f32(jld_stream_t stream, const float* data, int32_
 /*                  1 .. nstep-2 from their stored densities (one extra    */
 /*                  spectral forward per such layer) instead of keeping    */
 /*                  nstep-1 slots of 16 bytes per cell                      */
+/*           schedule choices (same results, different speed):             */
+/*           bit 4: x passes on radix-16 schedules where radix-8 ones fit  */
+/*           bits 5-6: narrowest pipelined tile, 0 automatic, 1/2/3 =      */
+/*                  4/8/16 columns                                         */
+/*           bits 7-8: binning tile edge (bit 2), 0/1/2 = 16/8/20 cells    */
 /*   out     device float64: [loss, d loss / d params ...]                 */
 /* Call jld_ldl_prepare_f32 (or one eager step) before capturing the step */
 /* into a CUDA graph; parameters are read from device memory, so a graph  */

@@ -8,11 +8,18 @@ that a single small box leaves idle; one `replay()` launches every box's
 step.  Parameters for all boxes live in one device buffer (one host->device
 copy per replay).
 
-Autotuning: for every distinct (mesh, particle count, kind) the first batch
-that meets it times each candidate configuration of the step (pipelined or
-generic FFT passes; plain, warp-aggregated or tiled scatters) for a few
-eager steps and keeps the fastest; the choice is cached for the process and
-optionally in a JSON file, so later batches and captures reuse it.
+Autotuning: for every distinct (mesh, particle count, kind, clustering
+level) the first batch that meets it times candidate configurations of the
+step for a few eager steps each and keeps the fastest.  The search runs in
+stages, each from the best configuration so far: the FFT passes (pipelined
+or generic) with the scatter method (plain, warp-aggregated or tiled
+atomics); then, for pipelined passes, the x passes' radix schedule (8 or 16)
+and the narrowest pipelined tile (4, 8 or 16 columns, or automatic); then,
+for tiled scatters, the binning tile edge (8, 16 or 20 cells).  The
+clustering level is the share of particles in cells that hold at least 8
+(below 1 %, below 10 %, above), so a clustered box of the same shape is
+tuned on its own.  Choices are cached for the process and optionally in a
+JSON file, so later batches and captures reuse them.
 
 There is no counterpart in the reference, which runs one box per process
 (model.py's JERALDModel); the batch is how the GPU build serves many small
@@ -36,11 +43,29 @@ CANDIDATES = [
     {"pipelined": True, "paint_method": "warp"},
 ]
 
+# keys of a tuned configuration (FusedLDL keyword arguments)
+TUNED = ("pipelined", "paint_method", "x_radix", "min_cols", "bin_tile")
+
 _CACHE: dict[str, dict] = {}
 
 
-def _key(nmesh, nparts, kind, nstep) -> str:
-    return f"{tuple(int(v) for v in nmesh)}:{int(nparts)}:{kind}:{int(nstep)}"
+def _key(nmesh, nparts, kind, nstep, level=0) -> str:
+    nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
+    return f"{tuple(int(v) for v in nm)}:{int(nparts)}:{kind}:{int(nstep)}:c{int(level)}"
+
+
+def clustering_level(pos: torch.Tensor, nmesh, box) -> int:
+    """0, 1 or 2: share of the particles in cells holding at least 8 of them
+    below 1 %, below 10 %, or above (cells of the paint's lower corner)."""
+    nm = torch.as_tensor(np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,)).copy(),
+                         device=pos.device)
+    bx = torch.as_tensor(np.broadcast_to(np.asarray(box, dtype=np.float64).reshape(-1), (3,)).copy(),
+                         device=pos.device)
+    cell = torch.floor(pos.double() / bx * nm).long() % nm
+    key = (cell[:, 0] * nm[1] + cell[:, 1]) * nm[2] + cell[:, 2]
+    occ = torch.bincount(key, minlength=int(nm.prod()))
+    share = float(occ[key].ge(8).double().mean())
+    return 0 if share < 0.01 else (1 if share < 0.1 else 2)
 
 
 def load_tuning(path: str) -> None:
@@ -57,15 +82,21 @@ def save_tuning(path: str) -> None:
 
 def autotune(nmesh, box, pos, target, params, nstep=2, kind="sm", L1=None, grad_mode="reference",
              candidates=None, reps: int = 3, device="cuda") -> dict:
-    """Fastest configuration of the fused step for this box shape (cached).
-    Each candidate runs one untimed and `reps` timed eager steps; the
-    candidates must agree on the loss (they compute the same step)."""
+    """Fastest configuration of the fused step for this box shape and
+    clustering level (cached).  Each candidate runs one untimed and `reps`
+    timed eager steps; the candidates must agree on the loss (they compute
+    the same step).  `candidates` replaces the staged search by one list."""
     nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
-    key = _key(nm, pos.shape[0], kind, nstep)
+    level = clustering_level(pos, nm, box)
+    key = _key(nm, pos.shape[0], kind, nstep, level)
     if key in _CACHE:
         return _CACHE[key]
-    best, times, losses = None, {}, []
-    for cand in (candidates or CANDIDATES):
+    times, losses = {}, []
+
+    def run(cand) -> float:
+        name = json.dumps(cand, sort_keys=True)
+        if name in times:
+            return times[name]
         step = FusedLDL(nm, box, pos.shape[0], nstep=nstep, kind=kind, L1=L1, grad_mode=grad_mode,
                         device=device, **cand)
         step(pos, params, target)
@@ -76,17 +107,28 @@ def autotune(nmesh, box, pos, target, params, nstep=2, kind="sm", L1=None, grad_
             loss, _ = step(pos, params, target)
         e1.record()
         torch.cuda.synchronize(device)
-        ms = e0.elapsed_time(e1) / reps
+        times[name] = e0.elapsed_time(e1) / reps
         losses.append(float(loss))
-        name = json.dumps(cand, sort_keys=True)
-        times[name] = ms
-        if best is None or ms < times[json.dumps(best, sort_keys=True)]:
-            best = cand
         del step
+        return times[name]
+
+    def best_of(cands):
+        return min(cands, key=run)
+
+    if candidates:
+        best = best_of(candidates)
+    else:
+        best = best_of(CANDIDATES)
+        if best["pipelined"]:
+            best = best_of([best, {**best, "x_radix": 16}])
+            best = best_of([best] + [{**best, "min_cols": c} for c in (4, 8, 16)])
+        if best["paint_method"] == "tiled":
+            best = best_of([best] + [{**best, "bin_tile": t} for t in (8, 20)])
     ref = losses[0]
     if any(abs(v - ref) > 1e-4 * abs(ref) for v in losses):
         raise RuntimeError(f"autotune candidates disagree on the loss: {losses}")
-    _CACHE[key] = {**best, "ms": times[json.dumps(best, sort_keys=True)], "timings": times}
+    _CACHE[key] = {**best, "ms": times[json.dumps(best, sort_keys=True)], "timings": times,
+                   "clustering_level": level}
     return _CACHE[key]
 
 
@@ -117,7 +159,7 @@ class FusedLDLBatch:
             if tune and not cfg:
                 t = autotune(b.nmesh, b.box, b.pos, b.target, _default_params(b), nstep=b.nstep, kind=b.kind,
                              L1=b.L1, grad_mode=b.grad_mode, device=self.device)
-                cfg = {"pipelined": t["pipelined"], "paint_method": t["paint_method"]}
+                cfg = {k: t[k] for k in TUNED if k in t}
             b.config = cfg
             st = FusedLDL(b.nmesh, b.box, b.pos.shape[0], nstep=b.nstep, kind=b.kind, L1=b.L1,
                           grad_mode=b.grad_mode, device=self.device, **cfg)

@@ -95,7 +95,7 @@ __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_
 template <typename T, bool BOX, bool STAGED = false>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? JLD_PAINT_MIN_CTAS : 3)
 paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
-             Grid3 g, T* __restrict__ out) {
+             Grid3 g, T* __restrict__ out, int* tick) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   // Clumps: a batch whose lower corners span at most three cells per axis
@@ -109,8 +109,10 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
   __shared__ __align__(16) float stage[STAGED ? 8 : 1][2][128];
   float* stg = stage[STAGED ? (threadIdx.x >> 5) : 0][0];
   const int nax[3] = {g.nx, g.ny, g.nz};
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t base0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
+  // the staged copies run two batches ahead in the grid-stride order
+  WarpBatches wb;
+  const int64_t base0 = wb.first(STAGED ? nullptr : tick);
+  const int64_t stride = wb.stride;
   auto issue = [&](int64_t b, int buf) {
     if (b + 32 <= n) {
       float* d = stg + buf * 128;
@@ -124,7 +126,7 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
     issue(base0 + stride, 1);
   }
   int kb = 0;
-  for (int64_t base = base0; base < n; base += stride, ++kb) {
+  for (int64_t base = base0; base < n; base = wb.next(base), ++kb) {
     const int64_t p = base + lane;
     const bool live = p < n;
     T q[3] = {T(0), T(0), T(0)};
@@ -693,7 +695,8 @@ static PosSrc<T> make_src(const T* pos, const T* box, int64_t nx, int64_t ny,
 template <typename T>
 static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* mass,
                       T mscalar, int64_t nx, int64_t ny, int64_t nz, const T* box,
-                      int method, T* out, const char* who, bool fast = false, bool clear = true) {
+                      int method, T* out, const char* who, bool fast = false, bool clear = true,
+                      int* tick = nullptr) {
   int s = check_common<T>(pos, nparts, out, nx, ny, nz, who);
   if (s) return s;
   if (box && !(box[0] > 0 && box[1] > 0 && box[2] > 0))
@@ -721,14 +724,14 @@ static int paint_impl(cudaStream_t st, const T* pos, int64_t nparts, const T* ma
       staged = use_staged && ((uintptr_t)pos & 15u) == 0 && ((uintptr_t)mass & 15u) == 0;
       if (staged) {
         const unsigned grid = resident_grid(paint_kernel<T, true, true>, nparts, block);
-        if (box) paint_kernel<T, true, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
-        else paint_kernel<T, false, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+        if (box) paint_kernel<T, true, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out, nullptr);
+        else paint_kernel<T, false, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out, nullptr);
       }
     }
     if (!staged) {
       const unsigned grid = resident_grid(paint_kernel<T, true>, nparts, block);
-      if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
-      else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out);
+      if (box) paint_kernel<T, true><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out, tick);
+      else paint_kernel<T, false><<<grid, block, 0, st>>>(src, nparts, mass, mscalar, g, out, tick);
     }
   }
   JLD_LAUNCH_CHECK(who);
@@ -798,8 +801,9 @@ static int readout3_impl(cudaStream_t st, const T* pos, int64_t nparts, const T*
 }
 
 int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny,
-                   int64_t nz, const float* box, int method, float* out) {
-  return paint_impl<float>(st, pos, n, nullptr, 1.0f, nx, ny, nz, box, method, out, "fused paint", true);
+                   int64_t nz, const float* box, int method, float* out, int* tick) {
+  return paint_impl<float>(st, pos, n, nullptr, 1.0f, nx, ny, nz, box, method, out, "fused paint", true, true,
+                           tick);
 }
 
 template <typename T>

@@ -66,9 +66,57 @@ inline unsigned resident_grid(K* func, int64_t n, int block, size_t smem = 0) {
 
 // Unit-mass CIC paint of box-unit positions into `out` (zeroed first); the
 // same kernels as jld_ppaint_box_f32 (method 0 atomics, 1 warp-aggregated)
-// with the division-free prelude (box_to_mesh_fast).
+// with the division-free prelude (box_to_mesh_fast).  tick: the launch's
+// WarpBatches counters (kTicksPerLaunch ints, zeroed) or nullptr.
 int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int64_t ny,
-                   int64_t nz, const float* box, int method, float* out);
+                   int64_t nz, const float* box, int method, float* out, int* tick = nullptr);
+
+// Batches of 32 consecutive particles walked by one warp of a persistent
+// particle kernel; every lane calls first() and next() together.
+// Without counters: the grid-stride order, batch w, w + W, w + 2W, ... for
+// global warp w of W.  With counters (kTickRegions ints kTickStride apart,
+// zero before the launch): units of kUnitBatches consecutive batches, unit u
+// in region u % kTickRegions; a warp's first unit is static (the
+// (w / kTickRegions)-th of region w % kTickRegions) and every later one is
+// its region counter's next value past the region's warp count, so warps
+// that start late (their SM partly held by other work: a host copy, another
+// box's step) take fewer units instead of holding the kernel up by a whole
+// share.  The regions keep the counters on separate cache lines.
+constexpr int kTickRegions = 32, kTickStride = 32, kUnitBatches = 8;
+constexpr int kTicksPerLaunch = kTickRegions * kTickStride;
+struct WarpBatches {
+  int* tick;
+  int64_t stride;    // grid-stride order: 32 W
+  int region, wr;    // counters: this warp's region, warps in the region
+  int64_t unit_end;  // counters: end of the current unit
+
+  __device__ __forceinline__ static int64_t unit_start(int region, int64_t q) {
+    return ((int64_t)region + (int64_t)kTickRegions * q) * (32 * kUnitBatches);
+  }
+  __device__ __forceinline__ int64_t first(int* tick_) {
+    const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    tick = W >= kTickRegions ? tick_ : nullptr;
+    stride = 32 * W;
+    if (!tick) return 32 * w;
+    region = (int)(w % kTickRegions);
+    wr = (int)((W - region + kTickRegions - 1) / kTickRegions);
+    const int64_t b = unit_start(region, w / kTickRegions);
+    unit_end = b + 32 * kUnitBatches;
+    return b;
+  }
+  __device__ __forceinline__ int64_t next(int64_t base) {
+    if (!tick) return base + stride;
+    base += 32;
+    if (base < unit_end) return base;
+    int q = 0;
+    if ((threadIdx.x & 31) == 0) q = wr + atomicAdd(tick + region * kTickStride, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    const int64_t b = unit_start(region, q);
+    unit_end = b + 32 * kUnitBatches;
+    return b;
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Mesh geometry passed by value to kernels.

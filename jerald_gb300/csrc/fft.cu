@@ -284,7 +284,7 @@ static int pipe_y_pass(cudaStream_t st, const Plan3<float>& pl, const FftPipe& f
     auto kern = sgn < 0 ? spass_kernel<Sch, 1, -1> : spass_kernel<Sch, 1, 1>;
     int r = ensure_smem(kern, fp.py.smem);
     if (r) return r;
-    kern<<<fp.py.grid, fp.py.nthr, fp.py.smem, st>>>(m, main, fp.py.g, pl.py.tw, err);
+    kern<<<fp.py.grid, fp.py.nthr, fp.py.smem, st>>>(m, main, fp.py.g, pl.py.tw, err, nullptr);
     return 0;
   });
   if (s) return s;
@@ -312,7 +312,7 @@ static int rfft3_pipe(cudaStream_t st, const Plan3<float>& pl, const FftPipe& fp
     int r = ensure_smem(kern, fp.z.smem);
     if (!r) r = persistent_grid(kern, fp.z.nthr, fp.z.smem, fp.z.zt.ntiles, &gz);
     if (r) return r;
-    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(data, SrcIdentity{}, fp.z.zt, pl.twr, main, pl.pz.tw, err);
+    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(data, SrcIdentity{}, fp.z.zt, pl.twr, main, pl.pz.tw, err, nullptr);
     return 0;
   });
   if (s) return s;
@@ -355,7 +355,7 @@ static int irfft3_pipe(cudaStream_t st, const Plan3<float>& pl, const FftPipe& f
     int r = ensure_smem(kern, fp.z.smem);
     if (!r) r = persistent_grid(kern, fp.z.nthr, fp.z.smem, fp.z.zt.ntiles, &gz);
     if (r) return r;
-    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(main, fp.z.zt, pl.twr, out, pl.pz.tw, err);
+    kern<<<gz, fp.z.nthr, fp.z.smem, st>>>(main, fp.z.zt, pl.twr, out, pl.pz.tw, err, nullptr);
     return 0;
   });
   if (s) return s;

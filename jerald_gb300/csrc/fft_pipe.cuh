@@ -60,6 +60,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Tile order of the persistent passes.  A CTA's first tile is blockIdx.x.
+// With a per-launch counter `tick` (zero before the launch) every later tile
+// is the counter's next value past the grid, so a CTA that starts late (its
+// SM partly held by other work: a copy kernel, another box's step) takes
+// fewer tiles instead of holding the pass up by a whole share.  Without a
+// counter the order is the static blockIdx.x + i * gridDim.x.
+__device__ __forceinline__ int next_tile(int* tick, int t) {
+  return tick ? (int)gridDim.x + atomicAdd(tick, 1) : t + (int)gridDim.x;
+}
+
 // Orders earlier generic-proxy accesses of shared memory before a later TMA
 // (async-proxy) write into it.
 __device__ __forceinline__ void fence_proxy_async_smem() {

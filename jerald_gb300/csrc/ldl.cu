@@ -20,22 +20,37 @@ struct LdlLayout {
   int64_t N, C, H;
   int nstep;
   size_t off_pos, off_xb, off_xb2, off_rho, off_S, off_g4, off_w[5], off_gb4, off_rb, off_part,
-      off_npix, off_err, off_xs0, off_keys, off_perm, off_tiles, off_g4x, off_s2, off_smu, off_dep, off_ctd,
-      total;
+      off_npix, off_err, off_tick, off_xs0, off_keys, off_perm, off_tiles, off_g4x, off_s2, off_smu, off_dep,
+      off_ctd, total;
+  int nticks, nptick;
   TileGeom tg;
   int64_t part_doubles;
 };
 
 static size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
 static constexpr int kMaxCellBlocks = 8192;
-static constexpr int kTileCells = 16;  // binning tile edge (cells)
-
 // Option bits of the fused step (jld_ldl_step_f32).
 constexpr int kOptWarpPaint = 1;   // warp-aggregated paint atomics
 constexpr int kOptGeneric = 2;     // generic (non-pipelined) FFT passes
 constexpr int kOptBinned = 4;      // per-step binning, tile-privatized scatters
 constexpr int kOptRecompute = 8;   // one force-mesh slot, recomputed in the adjoint
-constexpr int kOptAll = 15;
+// Schedule choices (same results, different speed; the batch autotuner
+// picks them per box shape):
+constexpr int kOptXRadix16 = 16;   // x passes on radix-16 schedules where radix-8 ones fit
+constexpr int kOptColsShift = 5;   // 2 bits: narrowest pipelined tile, 0 auto, 1/2/3 = 4/8/16 columns
+// 2 bits: binning tile edge, 0/1/2 = 16/8/20 cells (the adjoint's three
+// float windows of (t + 3)^3 cells must fit in shared memory: 146 KB at 20)
+constexpr int kOptBinShift = 7;
+constexpr int kOptAll = 511;
+
+static int opt_min_cols(int options) {
+  const int c = (options >> kOptColsShift) & 3;
+  return c ? 2 << c : 0;
+}
+static int opt_tile_cells(int options) {
+  const int c = (options >> kOptBinShift) & 3;
+  return c == 1 ? 8 : c == 2 ? 20 : 16;
+}
 
 // Force-mesh slots: the adjoint reads layer l's force mesh for l >= 1 only
 // (the first layer's input positions need no cotangent), so nstep - 1 slots
@@ -69,8 +84,14 @@ static LdlLayout ldl_layout(int nx, int ny, int nz, int64_t N, int nstep, int op
   L.off_part = o; o += al(sizeof(double) * L.part_doubles);    // per-block FP64 partials
   L.off_npix = o; o += al(sizeof(double) * 2);                 // 1 / Npixel
   L.off_err = o; o += al(sizeof(int) * 4);                     // pipelined-pass error word
+  // tile counters of the pipelined passes (next_tile), one per launch, then
+  // the particle kernels' batch counters (WarpBatches), kTicksPerLaunch per
+  // launch
+  L.nticks = 64 + 24 * nstep;
+  L.nptick = 3 * nstep + 2;
+  L.off_tick = o; o += al(sizeof(int) * (L.nticks + (size_t)L.nptick * kTicksPerLaunch));
   // particle binning: tile-ordered X_0, tile keys, order, tile counts/starts/fill
-  L.tg = make_tile_geom(nx, ny, nz, kTileCells, 1);
+  L.tg = make_tile_geom(nx, ny, nz, opt_tile_cells(options), 1);
   L.off_xs0 = L.off_keys = L.off_perm = L.off_tiles = 0;
   if (options & kOptBinned) {
     L.off_xs0 = o; o += al(sizeof(float) * 3 * N);
@@ -198,9 +219,19 @@ static int ldl_step(const StepArgs& a) {
   const float3 dwv = make_float3(bg.dw[0], bg.dw[1], bg.dw[2]);
   const size_t win1 = sizeof(float) * tg.wcells(), win3 = 3 * win1;
   const unsigned tgrid = (unsigned)std::min<int64_t>(tg.ntiles(), (int64_t)sm_count() * 8);
+  // zeroed work counters, one set per persistent launch: a tile counter per
+  // pipelined pass (next_tile), kTicksPerLaunch batch counters per particle
+  // kernel (WarpBatches); nullptr past the last set (static order)
+  int* ticks = (int*)(ws + L.off_tick);
+  JLD_CUDA_TRY(cudaMemsetAsync(ticks, 0, sizeof(int) * (L.nticks + (size_t)L.nptick * kTicksPerLaunch), st));
+  int nticks_used = 0, npticks_used = 0;
+  auto tick = [&]() -> int* { return nticks_used < L.nticks ? ticks + nticks_used++ : nullptr; };
+  auto ptick = [&]() -> int* {
+    return npticks_used < L.nptick ? ticks + L.nticks + (size_t)kTicksPerLaunch * npticks_used++ : nullptr;
+  };
   // Unit-mass paint of layer positions X into out (zeroed here).
   auto paint_into = [&](const float* X, float* out) -> int {
-    if (!a.binned) return paint_unit_f32(st, X, a.N, nx, ny, nz, a.box, a.paint_method, out);
+    if (!a.binned) return paint_unit_f32(st, X, a.N, nx, ny, nz, a.box, a.paint_method, out, ptick());
     JLD_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * L.C, st));
     int e = ensure_smem(tiled_paint_kernel, win1);
     if (e) return e;
@@ -252,11 +283,12 @@ static int ldl_step(const StepArgs& a) {
   // ---------------- pipelined (TMA-staged) strided passes, when the mesh qualifies
   int* err = (int*)(ws + L.off_err);
   JLD_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int) * 4, st));
-  const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0), py1 = pipe_geom(nx, ny, h, 1, 1);
-  const PipeGeom px16 = pipe_geom(nx, ny, h, 0, 1);
+  const int mc = opt_min_cols(a.options);
+  const PipeGeom py0 = pipe_geom(nx, ny, h, 1, 0, 16, 128, mc), py1 = pipe_geom(nx, ny, h, 1, 1, 16, 128, mc);
+  const PipeGeom px16 = pipe_geom(nx, ny, h, 0, 1, 16, 128, mc);
   // x passes: radix-8 schedules at <= 64 registers (twice the warps per SM)
   // where the tile fits, else the radix-16 ones
-  const PipeGeom px8 = pipe_geom(nx, ny, h, 0, 1, 8, 64);
+  const PipeGeom px8 = (a.options & kOptXRadix16) ? PipeGeom() : pipe_geom(nx, ny, h, 0, 1, 8, 64, mc);
   const PipeGeom& px1 = px8.ok ? px8 : px16;
   auto with_x = [&](auto&& body) { return px8.ok ? with_p2_8(nx, body) : with_p2(nx, body); };
   const bool pipe = a.use_pipe && py0.ok && py1.ok && px1.ok;
@@ -291,7 +323,7 @@ static int ldl_step(const StepArgs& a) {
       auto kern = sgn < 0 ? spass_kernel<Sch, 1, -1> : spass_kernel<Sch, 1, 1>;
       int r = ensure_smem(kern, py0.smem);
       if (r) return r;
-      kern<<<py0.grid, py0.nthr, py0.smem, st>>>(m, B, py0.g, pl.py.tw, err);
+      kern<<<py0.grid, py0.nthr, py0.smem, st>>>(m, B, py0.g, pl.py.tw, err, tick());
       return 0;
     });
     if (e) return e;
@@ -308,7 +340,7 @@ static int ldl_step(const StepArgs& a) {
 
   // x FFT in place on buffer B (main + nyq), for the HI kind's star-map
   // spectrum and its cotangent.
-  const PipeGeom pxs = pipe_geom(nx, ny, h, 0, 0);
+  const PipeGeom pxs = pipe_geom(nx, ny, h, 0, 0, 16, 128, mc);
   auto xpass = [&](float2* B, int sgn) -> int {
     LineJob<float> jm = job_x_internal<float>(pl, B, false), jn = job_x_internal<float>(pl, B + nyq_off, true),
                    none;
@@ -321,7 +353,7 @@ static int ldl_step(const StepArgs& a) {
       auto kern = sgn < 0 ? spass_kernel<Sch, 0, -1> : spass_kernel<Sch, 0, 1>;
       int r = ensure_smem(kern, pxs.smem);
       if (r) return r;
-      kern<<<pxs.grid, pxs.nthr, pxs.smem, st>>>(m, B, pxs.g, pl.px.tw, err);
+      kern<<<pxs.grid, pxs.nthr, pxs.smem, st>>>(m, B, pxs.g, pl.px.tw, err, tick());
       return 0;
     });
     if (e) return e;
@@ -342,7 +374,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(kern, zr2c.smem);
         if (!r) r = persistent_grid(kern, zr2c.nthr, zr2c.smem, zr2c.zt.ntiles, &gz);
         if (r) return r;
-        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(a.starmap, sp, zr2c.zt, pl.twr, S2, pl.pz.tw, err);
+        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(a.starmap, sp, zr2c.zt, pl.twr, S2, pl.pz.tw, err, tick());
         return 0;
       });
       if (s2) return s2;
@@ -377,7 +409,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(kern, zc2r1.smem);
         if (!r) r = persistent_grid(kern, zc2r1.nthr, zc2r1.smem, zc2r1.zt.ntiles, &gz);
         if (r) return r;
-        kern<<<gz, zc2r1.nthr, zc2r1.smem, st>>>(Wc, zc2r1.zt, pl.twr, cts, pl.pz.tw, err);
+        kern<<<gz, zc2r1.nthr, zc2r1.smem, st>>>(Wc, zc2r1.zt, pl.twr, cts, pl.pz.tw, err, tick());
         return 0;
       });
       if (s2) return s2;
@@ -410,7 +442,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(kern, zr2c.smem);
         if (!r) r = persistent_grid(kern, zr2c.nthr, zr2c.smem, zr2c.zt.ntiles, &gz);
         if (r) return r;
-        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(rho_l, src, zr2c.zt, pl.twr, W[0], pl.pz.tw, err);
+        kern<<<gz, zr2c.nthr, zr2c.smem, st>>>(rho_l, src, zr2c.zt, pl.twr, W[0], pl.pz.tw, err, tick());
         return 0;
       });
       if (s) return s;
@@ -427,7 +459,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(xfilt_pipe_kernel<Sch>, px1.smem);
         if (r) return r;
         xfilt_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(mA, px1.g, kt, prm, a.kind, scale, S_l, W[1],
-                                                                    W[2], pl.px.tw, err, S2_l);
+                                                                    W[2], pl.px.tw, err, S2_l, tick());
         return 0;
       });
       if (s) return s;
@@ -451,7 +483,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(yinv3_pipe_kernel<Sch>, py0.smem);
         if (r) return r;
         yinv3_pipe_kernel<Sch><<<py0.grid, py0.nthr, py0.smem, st>>>(m0, m1, py0.g, kt, W[3], W[0], W[4],
-                                                                    pl.py.tw, err);
+                                                                    pl.py.tw, err, tick());
         return 0;
       });
       if (s) return s;
@@ -475,7 +507,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(kern, zc2r3.smem);
         if (!r) r = persistent_grid(kern, zc2r3.nthr, zc2r3.smem, zc2r3.zt.ntiles, &gz);
         if (r) return r;
-        kern<<<gz, zc2r3.nthr, zc2r3.smem, st>>>(W[3], W[0], W[4], zc2r3.zt, pl.twr, g4_l, pl.pz.tw, err);
+        kern<<<gz, zc2r3.nthr, zc2r3.smem, st>>>(W[3], W[0], W[4], zc2r3.zt, pl.twr, g4_l, pl.pz.tw, err, tick());
         return 0;
       });
     } else {
@@ -506,7 +538,8 @@ static int ldl_step(const StepArgs& a) {
     float4* g4_l = g4_of(l);
     if (hi && (s = star_spectrum(l, (float2*)(ws + L.off_s2) + (size_t)L.H * l))) return s;
     if ((s = force_mesh(l, g4_l))) return s;
-    update_kernel<<<resident_grid(update_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l, Xs + (size_t)3 * a.N * l);
+    update_kernel<<<resident_grid(update_kernel, a.N, pblock), pblock, 0, st>>>(Xl(l), a.N, bg, g, g4_l,
+                                                                              Xs + (size_t)3 * a.N * l, ptick());
     JLD_LAUNCH_CHECK("update_kernel");
     if ((s = paint_into(Xl(l + 1), rho + (size_t)L.C * (l + 1)))) return s;  // the final map for l = nstep-1
   }
@@ -621,9 +654,11 @@ static int ldl_step(const StepArgs& a) {
       // the first layer's input positions are data: scatter only
       const float* Xbp = (l == a.nstep - 1) ? nullptr : Xb;
       if (l > 0)
-        bwd_fused_kernel<true><<<resident_grid(bwd_fused_kernel<true>, a.N, pblock), pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
+        bwd_fused_kernel<true><<<resident_grid(bwd_fused_kernel<true>, a.N, pblock), pblock, 0, st>>>(
+            Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2, ptick());
       else
-        bwd_fused_kernel<false><<<resident_grid(bwd_fused_kernel<false>, a.N, pblock), pblock, 0, st>>>(Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2);
+        bwd_fused_kernel<false><<<resident_grid(bwd_fused_kernel<false>, a.N, pblock), pblock, 0, st>>>(
+            Xl(l + 1), rb, Xbp, Xl(l), a.N, bg, g, g4_l, gb4, Xb2, ptick());
       JLD_LAUNCH_CHECK("bwd_fused_kernel");
     }
     if (zr2c3.ok) {
@@ -634,7 +669,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(kern, zr2c3.smem);
         if (!r) r = persistent_grid(kern, zr2c3.nthr, zr2c3.smem, zr2c3.zt.ntiles, &gz);
         if (r) return r;
-        kern<<<gz, zr2c3.nthr, zr2c3.smem, st>>>(gb4, zr2c3.zt, pl.twr, kt.cz, W[0], W[1], W[2], pl.pz.tw, err);
+        kern<<<gz, zr2c3.nthr, zr2c3.smem, st>>>(gb4, zr2c3.zt, pl.twr, kt.cz, W[0], W[1], W[2], pl.pz.tw, err, tick());
         return 0;
       });
     } else {
@@ -657,7 +692,7 @@ static int ldl_step(const StepArgs& a) {
         int r = ensure_smem(yfwd_comb_pipe_kernel<Sch>, py1.smem);
         if (r) return r;
         yfwd_comb_pipe_kernel<Sch><<<py1.grid, py1.nthr, py1.smem, st>>>(m0, m1, m2, py1.g, kt, W[0], W[3],
-                                                                        pl.py.tw, err);
+                                                                        pl.py.tw, err, tick());
         return 0;
       });
       if (s) return s;
@@ -684,7 +719,7 @@ static int ldl_step(const StepArgs& a) {
         if (r) return r;
         xbwd_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(m0, m1, m2, px1.g, kt, prm, a.kind, a.mode,
                                                                    scale, W[1], part, pl.px.tw, err,
-                                                                   hi ? W[2] : nullptr);
+                                                                   hi ? W[2] : nullptr, tick());
         return 0;
       });
       if (s) return s;
@@ -718,7 +753,7 @@ static int ldl_step(const StepArgs& a) {
         if (!r) r = persistent_grid(kern, zadj.nthr, zadj.smem, zadj.zt.ntiles, &adj_blocks);
         if (r) return r;
         kern<<<adj_blocks, zadj.nthr, zadj.smem, st>>>(W[1], zadj.zt, pl.twr, rho_l, prm, fact,
-                                                       l > 0 ? rb : nullptr, part, pl.pz.tw, err);
+                                                       l > 0 ? rb : nullptr, part, pl.pz.tw, err, tick());
         return 0;
       });
     } else {
@@ -796,7 +831,8 @@ static int step_entry(jld_stream_t stream, const float* pos, int64_t nparts, int
   if (L1 != 0 && L1 != 1) return set_error(JLD_ERR_ARG, "%s: L1 must be 0 or 1", who);
   if (grad_mode != 0 && grad_mode != 1)
     return set_error(JLD_ERR_ARG, "%s: grad_mode must be 0 (reference) or 1 (true)", who);
-  if (options & ~kOptAll) return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
+  if ((options & ~kOptAll) || ((options >> kOptBinShift) & 3) == 3)
+    return set_error(JLD_ERR_ARG, "%s: unknown option bits 0x%x", who, options);
   if ((options & kOptBinned) && nparts > INT32_MAX)
     return set_error(JLD_ERR_UNSUPPORTED, "%s: binning needs fewer than 2^31 particles", who);
   const int paint_method = (options & kOptWarpPaint) ? 1 : 0;

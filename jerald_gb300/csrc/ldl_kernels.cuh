@@ -450,16 +450,24 @@ __device__ __forceinline__ float wprod(const float lo[3], const float hi[3], int
 #endif
 __global__ void __launch_bounds__(256, JLD_UPD_MIN_CTAS)
 update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
-              const float4* __restrict__ g4, float* __restrict__ Xn) {
-  // the next iteration's position is loaded one iteration ahead
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+              const float4* __restrict__ g4, float* __restrict__ Xn, int* tick) {
+  // warps walk batches of 32 particles (WarpBatches); the next batch's
+  // position is loaded one batch ahead
+  const int lane = threadIdx.x & 31;
+  WarpBatches wb;
+  int64_t base = wb.first(tick);
   float nr[3] = {0.f, 0.f, 0.f};
-  if (p < n) { nr[0] = __ldg(X + 3 * p); nr[1] = __ldg(X + 3 * p + 1); nr[2] = __ldg(X + 3 * p + 2); }
-  for (; p < n; p += stride) {
+  if (base + lane < n) {
+    const int64_t p = base + lane;
+    nr[0] = __ldg(X + 3 * p); nr[1] = __ldg(X + 3 * p + 1); nr[2] = __ldg(X + 3 * p + 2);
+  }
+  for (; base < n;) {
+    const int64_t p = base + lane;
     const float r[3] = {nr[0], nr[1], nr[2]};
-    const int64_t pn = p + stride;
+    base = wb.next(base);
+    const int64_t pn = base + lane;
     if (pn < n) { nr[0] = __ldg(X + 3 * pn); nr[1] = __ldg(X + 3 * pn + 1); nr[2] = __ldg(X + 3 * pn + 2); }
+    if (p >= n) continue;
     Corners<float> c;
     float lo[3], hi[3];
     {
@@ -532,10 +540,10 @@ template <bool GATHER>
 __global__ void __launch_bounds__(256, JLD_BWD_MIN_CTAS)
 bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, const float* __restrict__ Xbp,
                  const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g, const float4* __restrict__ g4,
-                 float4* __restrict__ gb4, float* __restrict__ Xb) {
+                 float4* __restrict__ gb4, float* __restrict__ Xb, int* tick) {
   const unsigned full = 0xffffffffu;
-  const int64_t wstride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += wstride) {
+  WarpBatches wb;
+  for (int64_t base = wb.first(tick); base < n; base = wb.next(base)) {
     const bool live = base + (threadIdx.x & 31) < n;
     const int64_t p = live ? base + (threadIdx.x & 31) : n - 1;
     float v[3];

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, const float* __restrict__ params,
                   int kind, float scale, float2* __restrict__ S, float2* __restrict__ T0,
                   float2* __restrict__ T1, const float2* __restrict__ tw, int* err,
-                  const float2* __restrict__ S2) {
+                  const float2* __restrict__ S2, int* tick) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int cky[64], ckz[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -33,27 +33,30 @@ xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, c
   PipeSmem s = pipe_smem(smraw, tile_elems, 1, 1);
   if (tid == 0) { mbar_init(s.bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  if (tid == 0 && ntl > 0) issue_tile<0>(&mA, s.slot[0], s.bar, g, blockIdx.x);
+  __shared__ int s_next;
+  int t = blockIdx.x;
+  if (tid == 0 && t < g.ntiles) issue_tile<0>(&mA, s.slot[0], s.bar, g, t);
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3), nu = __ldg(params + 4);
   const float a = pot_coef(kind) * alpha * scale;
   ColWork wk{s.work, g.cols};
   ColWork ac{s.acc, g.cols};
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
+  for (int i = 0; t < g.ntiles; ++i) {
     bool ok = mbar_wait_bounded(s.bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 2); return; }
     xcols(g, t, cky, ckz, tid);
     const int64_t base = tile_base<0>(g, t);
     const float2* slot = s.slot[0];
-    const bool more = i + 1 < ntl;
     auto in = [&](int c, int j) { return slot[j * g.cols + c]; };
     auto keep = [&](int c, int j, float2 v) {
       S[base + c + (int64_t)j * g.es] = v;
       ac.at(c, j) = v;
     };
     auto rel = [&]() {
-      if (tid == 0 && more) { fence_proxy_async_smem(); issue_tile<0>(&mA, s.slot[0], s.bar, g, t + gridDim.x); }
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < g.ntiles) { fence_proxy_async_smem(); issue_tile<0>(&mA, s.slot[0], s.bar, g, nt); }
+      }
     };
     p2_run_rel<Sch, true>(wk, in, keep, rel, tw, -1, g.cshift, tid, nthr);
     __syncthreads();
@@ -80,6 +83,7 @@ xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, c
     auto st1 = [&](int c, int j, float2 v) { T1[base + c + (int64_t)j * g.es] = v; };
     p2_run<Sch, true>(wk, inQ, st1, tw, +1, g.cshift, tid, nthr);
     __syncthreads();
+    t = s_next;
   }
 }
 
@@ -89,23 +93,22 @@ template <class Sch>
 __global__ void __launch_bounds__(512)
 yinv3_pipe_kernel(const __grid_constant__ CUtensorMap mT0, const __grid_constant__ CUtensorMap mT1, SGeom g,
                   KTables kt, float2* __restrict__ Gx, float2* __restrict__ Gy, float2* __restrict__ Gz,
-                  const float2* __restrict__ tw, int* err) {
+                  const float2* __restrict__ tw, int* err, int* tick) {
   extern __shared__ __align__(128) unsigned char smraw[];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int tile_elems = g.lines * g.cols;
   PipeSmem s = pipe_smem(smraw, tile_elems, 1, 0);
   if (tid == 0) { mbar_init(s.bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  if (tid == 0 && ntl > 0) issue_tile<1>(&mT0, s.slot[0], s.bar, g, blockIdx.x);
+  __shared__ int s_next;
+  int t = blockIdx.x;
+  if (tid == 0 && t < g.ntiles) issue_tile<1>(&mT0, s.slot[0], s.bar, g, t);
   ColWork wk{s.work, g.cols};
   const float2* slot = s.slot[0];
   int phase = 0;
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
+  for (int i = 0; t < g.ntiles; ++i) {
     const int64_t base = tile_base<1>(g, t);
     const int kz0 = (int)(base % g.h);
-    const bool more = i + 1 < ntl;
     // item T0
     bool ok = mbar_wait_bounded(s.bar, (uint32_t)(phase++ & 1));
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 3); return; }
@@ -132,10 +135,14 @@ yinv3_pipe_kernel(const __grid_constant__ CUtensorMap mT0, const __grid_constant
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 3); return; }
     auto stX = [&](int c, int j, float2 v) { Gx[base + c + (int64_t)j * g.es] = v; };
     auto relN = [&]() {
-      if (tid == 0 && more) { fence_proxy_async_smem(); issue_tile<1>(&mT0, s.slot[0], s.bar, g, t + gridDim.x); }
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < g.ntiles) { fence_proxy_async_smem(); issue_tile<1>(&mT0, s.slot[0], s.bar, g, nt); }
+      }
     };
     p2_run_rel<Sch, true>(wk, in0, stX, relN, tw, +1, g.cshift, tid, nthr);
-    __syncthreads();
+    __syncthreads();    t = s_next;
   }
 }
 
@@ -145,24 +152,23 @@ template <class Sch>
 __global__ void __launch_bounds__(512)
 yfwd_comb_pipe_kernel(const __grid_constant__ CUtensorMap mAx, const __grid_constant__ CUtensorMap mAy,
                       const __grid_constant__ CUtensorMap mAz, SGeom g, KTables kt, float2* __restrict__ Bx,
-                      float2* __restrict__ D, const float2* __restrict__ tw, int* err) {
+                      float2* __restrict__ D, const float2* __restrict__ tw, int* err, int* tick) {
   extern __shared__ __align__(128) unsigned char smraw[];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int tile_elems = g.lines * g.cols;
   PipeSmem s = pipe_smem(smraw, tile_elems, 1, 1);
   if (tid == 0) { mbar_init(s.bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  if (tid == 0 && ntl > 0) issue_tile<1>(&mAx, s.slot[0], s.bar, g, blockIdx.x);
+  __shared__ int s_next;
+  int t = blockIdx.x;
+  if (tid == 0 && t < g.ntiles) issue_tile<1>(&mAx, s.slot[0], s.bar, g, t);
   ColWork wk{s.work, g.cols};
   ColWork ac{s.acc, g.cols};
   const float2* slot = s.slot[0];
   auto in0 = [&](int c, int j) { return slot[j * g.cols + c]; };
   int phase = 0;
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
+  for (int i = 0; t < g.ntiles; ++i) {
     const int64_t base = tile_base<1>(g, t);
-    const bool more = i + 1 < ntl;
     bool ok = mbar_wait_bounded(s.bar, (uint32_t)(phase++ & 1));
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 4); return; }
     auto stB = [&](int c, int j, float2 v) { Bx[base + c + (int64_t)j * g.es] = v; };
@@ -185,10 +191,14 @@ yfwd_comb_pipe_kernel(const __grid_constant__ CUtensorMap mAx, const __grid_cons
       D[base + c + (int64_t)j * g.es] = make_float2(u.x + v.x, u.y + v.y);
     };
     auto relN = [&]() {
-      if (tid == 0 && more) { fence_proxy_async_smem(); issue_tile<1>(&mAx, s.slot[0], s.bar, g, t + gridDim.x); }
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < g.ntiles) { fence_proxy_async_smem(); issue_tile<1>(&mAx, s.slot[0], s.bar, g, nt); }
+      }
     };
     p2_run_rel<Sch, true>(wk, in0, stD, relN, tw, -1, g.cshift, tid, nthr);
-    __syncthreads();
+    __syncthreads();    t = s_next;
   }
 }
 
@@ -199,7 +209,7 @@ __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant__ CUtensorMap mD,
                  const __grid_constant__ CUtensorMap mS, SGeom g, KTables kt, const float* __restrict__ params,
                  int kind, int mode, float scale, float2* __restrict__ Vout, double* __restrict__ partials,
-                 const float2* __restrict__ tw, int* err, float2* __restrict__ Wout) {
+                 const float2* __restrict__ tw, int* err, float2* __restrict__ Wout, int* tick) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int cky[64], ckz[64];
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -207,8 +217,9 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
   PipeSmem s = pipe_smem(smraw, tile_elems, 1, 1);
   if (tid == 0) { mbar_init(s.bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  if (tid == 0 && ntl > 0) issue_tile<0>(&mBx, s.slot[0], s.bar, g, blockIdx.x);
+  __shared__ int s_next;
+  int t = blockIdx.x;
+  if (tid == 0 && t < g.ntiles) issue_tile<0>(&mBx, s.slot[0], s.bar, g, t);
   const float alpha = __ldg(params + 0), kh = __ldg(params + 2), kl = __ldg(params + 3), nu = __ldg(params + 4);
   const float pc = pot_coef(kind);
   const float a1 = pc * scale;
@@ -221,10 +232,8 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
   KahanF acc[4];
   int phase = 0;
   bool failed = false;
-  for (int i = 0; i < ntl && !failed; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
+  for (int i = 0; t < g.ntiles && !failed; ++i) {
     const int64_t base = tile_base<0>(g, t);
-    const bool more = i + 1 < ntl;
     bool ok = mbar_wait_bounded(s.bar, (uint32_t)(phase++ & 1));
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 5); failed = true; break; }
     xcols(g, t, cky, ckz, tid);
@@ -267,11 +276,15 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
       ac.at(c, j) = make_float2(W.x * vm, W.y * vm);
     }
     __syncthreads();
-    if (tid == 0 && more) { fence_proxy_async_smem(); issue_tile<0>(&mBx, s.slot[0], s.bar, g, t + gridDim.x); }
+    if (tid == 0) {
+      const int nt = next_tile(tick, t);
+      s_next = nt;
+      if (nt < g.ntiles) { fence_proxy_async_smem(); issue_tile<0>(&mBx, s.slot[0], s.bar, g, nt); }
+    }
     auto inV = [&](int c, int j) { return ac.at(c, j); };
     auto stV = [&](int c, int j, float2 v) { Vout[base + c + (int64_t)j * g.es] = v; };
     p2_run<Sch, true>(wk, inV, stV, tw, +1, g.cshift, tid, nthr);
-    __syncthreads();
+    __syncthreads();    t = s_next;
   }
   if (failed) return;
   block_reduce_kahan<4>(acc, partials, 4);

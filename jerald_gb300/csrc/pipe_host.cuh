@@ -74,7 +74,7 @@ struct PipeGeom {
 
 // E = values per thread per line of the schedule (16: P2For, 8: P2For8);
 // regs = registers per thread the kernel is built for.
-inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, int regs = 128) {
+inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, int regs = 128, int min_cols_req = 0) {
   PipeGeom p;
   const int lines = ax == 1 ? ny : nx;
   if (lines < 16 || lines > 2048 || (lines & (lines - 1)) || h < 2 || (h & 1)) return p;
@@ -90,14 +90,15 @@ inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, i
   // (4 MiB apart for the x pass at 1024^3).  At 1024 lines 64-byte pieces
   // at one CTA per SM beat 32-byte pieces at two: the 1024^3 r2c took
   // 8.58 instead of 12.28 ms; 512^3 and 256^3 (which get 8 or 16 columns at
-  // two CTAs anyway) did not change.  JLD_PIPE_MIN_COLS = 4, 8 or 16
-  // overrides the choice (a tuning knob; results are the same).
+  // two CTAs anyway) did not change.  min_cols_req (4, 8 or 16; the fused
+  // step's tuning option) or else JLD_PIPE_MIN_COLS = 4, 8 or 16 overrides
+  // the choice (results are the same).
   static const int min_cols_env = [] {
     const char* e = getenv("JLD_PIPE_MIN_COLS");
     const int v = e ? atoi(e) : 0;
     return (v == 4 || v == 8 || v == 16) ? v : 0;
   }();
-  const int min_cols = min_cols_env ? min_cols_env : (lines >= 1024 ? 8 : 4);
+  const int min_cols = min_cols_req ? min_cols_req : min_cols_env ? min_cols_env : (lines >= 1024 ? 8 : 4);
   int cols = 16;
   while (cols >= min_cols && !fits(cols, 112 * 1024)) cols >>= 1;
   if (cols < min_cols) {

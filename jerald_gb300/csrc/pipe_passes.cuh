@@ -4,10 +4,10 @@
 //
 // Tiles are `cols` consecutive kz (y passes) or (y, kz) columns (x passes) by
 // the whole line; a tile is one TMA load (two or more 256-line boxes).  Each
-// CTA is persistent over tiles t = blockIdx.x + i * gridDim.x and keeps one
-// staging slot: the load of tile i+1 is issued as soon as the first FFT
-// stage of tile i has copied the slot into the work buffer, so it overlaps
-// the remaining stages and the epilogue of tile i.
+// CTA is persistent over tiles (blockIdx.x first, then the order of
+// next_tile) and keeps one staging slot: the load of its next tile is issued
+// as soon as the first FFT stage of the current one has copied the slot into
+// the work buffer, so it overlaps the remaining stages and the epilogue.
 #pragma once
 
 #include "fft_pipe.cuh"
@@ -79,8 +79,9 @@ __device__ __forceinline__ void pipe_error(int* err, int code) {
 template <class Sch, int AX, int SGN>
 __global__ void __launch_bounds__(512)
 spass_kernel(const __grid_constant__ CUtensorMap m_in, float2* out, SGeom g, const float2* __restrict__ tw,
-             int* err) {
+             int* err, int* tick) {
   extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ int s_next;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int tile_elems = g.lines * g.cols;
   PipeSmem s = pipe_smem(smraw, tile_elems, 1, 0);
@@ -89,26 +90,29 @@ spass_kernel(const __grid_constant__ CUtensorMap m_in, float2* out, SGeom g, con
     mbar_fence_init();
   }
   __syncthreads();
-  const int ntl = (g.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-  if (tid == 0 && ntl > 0) issue_tile<AX>(&m_in, s.slot[0], s.bar, g, blockIdx.x);
+  int t = blockIdx.x;
+  if (tid == 0 && t < g.ntiles) issue_tile<AX>(&m_in, s.slot[0], s.bar, g, t);
   ColWork wk{s.work, g.cols};
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
+  for (int i = 0; t < g.ntiles; ++i) {
     bool ok = mbar_wait_bounded(s.bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) { if (tid == 0) pipe_error(err, 1); return; }
     const float2* slot = s.slot[0];
     const int64_t base = tile_base<AX>(g, t);
-    const bool more = i + 1 < ntl;
     auto in = [&](int c, int j) { return slot[j * g.cols + c]; };
     auto st = [&](int c, int j, float2 v) { out[base + c + (int64_t)j * g.es] = v; };
     auto release = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue_tile<AX>(&m_in, s.slot[0], s.bar, g, t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < g.ntiles) {
+          fence_proxy_async_smem();
+          issue_tile<AX>(&m_in, s.slot[0], s.bar, g, nt);
+        }
       }
     };
     p2_run_rel<Sch, true>(wk, in, st, release, tw, SGN, g.cshift, tid, nthr);
     __syncthreads();
+    t = s_next;
   }
 }
 

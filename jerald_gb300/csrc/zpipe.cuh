@@ -18,7 +18,7 @@ template <class Sch>
 __global__ void __launch_bounds__(512)
 zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, const float2* __restrict__ Gz,
                   ZTile zt, const float2* __restrict__ twr, float4* __restrict__ g4,
-                  const float2* __restrict__ tw, int* err) {
+                  const float2* __restrict__ tw, int* err, int* tick) {
   using Z = ZShape<Sch>;
   constexpr int H = Z::H;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -31,7 +31,8 @@ zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, 
   if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
   __syncthreads();
   const float2* src[3] = {Gx, Gy, Gz};
-  const int ntl = z_my_tiles(zt.ntiles);
+  __shared__ int s_next;
+  int t = blockIdx.x;
   auto issue = [&](int t) {
     const uint32_t b0 = (uint32_t)R * H * 8u, b1 = (uint32_t)R * 8u;
     mbar_arrive_expect_tx(bar, 3u * (b0 + b1));
@@ -41,11 +42,9 @@ zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, 
       bulk_load_1d(nq + d * R, src[d] + zt.nyq_off + (int64_t)t * R, b1, bar);
     }
   };
-  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  if (tid == 0 && t < zt.ntiles) issue(t);
   RowWork<Z::PSH> wk{work, Z::LDW};
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
-    const bool more = i + 1 < ntl;
+  for (int i = 0; t < zt.ntiles; ++i) {
     const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) {
       if (tid == 0 && err) atomicExch(err, 7);
@@ -53,9 +52,13 @@ zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, 
     }
     auto in0 = [&](int c, int k) { return c2r_pack_tile(slot, nq, H, c, k, twr); };
     auto rel = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue(t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < zt.ntiles) {
+          fence_proxy_async_smem();
+          issue(nt);
+        }
       }
     };
     p2_rows_to_work<Sch>(wk, in0, rel, tw, +1, tid, nthr);
@@ -69,6 +72,7 @@ zc2r3_pipe_kernel(const float2* __restrict__ Gx, const float2* __restrict__ Gy, 
       o[1] = make_float4(a.y, b.y, e.y, 0.f);
     }
     __syncthreads();
+    t = s_next;
   }
 }
 
@@ -84,7 +88,7 @@ __global__ void __launch_bounds__(kZadjThreads, 6)
 zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restrict__ twr,
                      const float* __restrict__ rho_paint, const float* __restrict__ params, float fact,
                      float* __restrict__ rb, double* __restrict__ partials, const float2* __restrict__ tw,
-                     int* err) {
+                     int* err, int* tick) {
   using Z = ZShape<Sch>;
   constexpr int H = Z::H;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -96,20 +100,19 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
   const int tid = threadIdx.x, nthr = blockDim.x;
   if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = z_my_tiles(zt.ntiles);
+  __shared__ int s_next;
+  int t = blockIdx.x;
   auto issue = [&](int t) {
     const uint32_t b0 = (uint32_t)R * H * 8u, b1 = (uint32_t)R * 8u;
     mbar_arrive_expect_tx(bar, b0 + b1);
     bulk_load_1d(slot, V + (int64_t)t * R * H, b0, bar);
     bulk_load_1d(nq, V + zt.nyq_off + (int64_t)t * R, b1, bar);
   };
-  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  if (tid == 0 && t < zt.ntiles) issue(t);
   RowWork<Z::PSH> wk{work, Z::LDW};
   const float gamma = __ldg(params + 1);
   KahanF acc[1];
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
-    const bool more = i + 1 < ntl;
+  for (int i = 0; t < zt.ntiles; ++i) {
     const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) {
       if (tid == 0 && err) atomicExch(err, 8);
@@ -117,9 +120,13 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
     }
     auto in0 = [&](int c, int k) { return c2r_pack_tile(slot, nq, H, c, k, twr); };
     auto rel = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue(t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < zt.ntiles) {
+          fence_proxy_async_smem();
+          issue(nt);
+        }
       }
     };
     p2_rows_to_work<Sch>(wk, in0, rel, tw, +1, tid, nthr);
@@ -144,6 +151,7 @@ zc2r_adj_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __res
       if (rb) *reinterpret_cast<float2*>(rb + e) = make_float2(o[0], o[1]);
     }
     __syncthreads();
+    t = s_next;
   }
   block_reduce_kahan<1>(acc, partials, 1);
 }
@@ -160,7 +168,7 @@ template <class Sch>
 __global__ void __launch_bounds__(kZr2c3Threads, 3)
 zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __restrict__ twr,
                   const float* __restrict__ cz, float2* __restrict__ Ax, float2* __restrict__ Ay,
-                  float2* __restrict__ Az, const float2* __restrict__ tw, int* err) {
+                  float2* __restrict__ Az, const float2* __restrict__ tw, int* err, int* tick) {
   using Z = ZShape<Sch>;
   constexpr int H = Z::H;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -172,17 +180,16 @@ zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __rest
   if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
   __syncthreads();
   const uint32_t bytes = (uint32_t)R * 2 * H * 16u;
-  const int ntl = z_my_tiles(zt.ntiles);
+  __shared__ int s_next;
+  int t = blockIdx.x;
   auto issue = [&](int t) {
     mbar_arrive_expect_tx(bar, bytes);
     bulk_load_1d(slot, gb4 + (int64_t)t * R * 2 * H, bytes, bar);
   };
-  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  if (tid == 0 && t < zt.ntiles) issue(t);
   RowWork<Z::PSH> wk{work, Z::LDW};
   float2* dst[3] = {Ax, Ay, Az};
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
-    const bool more = i + 1 < ntl;
+  for (int i = 0; t < zt.ntiles; ++i) {
     const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) {
       if (tid == 0 && err) atomicExch(err, 9);
@@ -194,9 +201,13 @@ zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __rest
       return d == 0 ? make_float2(a.x, b.x) : d == 1 ? make_float2(a.y, b.y) : make_float2(a.z, b.z);
     };
     auto rel = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue(t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < zt.ntiles) {
+          fence_proxy_async_smem();
+          issue(nt);
+        }
       }
     };
     p2_rows_to_work<Sch>(wk, in0, rel, tw, -1, tid, nthr);
@@ -225,6 +236,7 @@ zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __rest
       else if (H - k != k) o[row * H + (H - k)] = make_float2(xhk.x * s2, xhk.y * s2);
     }
     __syncthreads();
+    t = s_next;
   }
 }
 

@@ -74,11 +74,6 @@ __device__ __forceinline__ float2 c2r_pack_tile(const float2* slot, const float2
   return make_float2(a.x - t.y, a.y + t.x);
 }
 
-// Number of tiles of this CTA (grid-stride over tiles).
-__device__ __forceinline__ int z_my_tiles(int ntiles) {
-  return (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-}
-
 // ---------------------------------------------------------------------------
 // Forward z pass (r2c) of real rows with the source map applied on load:
 // main[row][k] (k < h) and nyq[row] = X[h].
@@ -86,7 +81,7 @@ constexpr int kZr2cThreads = 256;  // CTA size cap of its geometry
 template <class Sch, class Src>
 __global__ void __launch_bounds__(512)
 zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* __restrict__ twr,
-                 float2* __restrict__ main, const float2* __restrict__ tw, int* err) {
+                 float2* __restrict__ main, const float2* __restrict__ tw, int* err, int* tick) {
   using Z = ZShape<Sch>;
   constexpr int H = Z::H;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -98,17 +93,16 @@ zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* 
   if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
   __syncthreads();
   const uint32_t bytes = (uint32_t)R * H * 8u;
-  const int ntl = z_my_tiles(zt.ntiles);
+  __shared__ int s_next;
+  int t = blockIdx.x;
   auto issue = [&](int t) {
     mbar_arrive_expect_tx(bar, bytes);
     bulk_load_1d(slot, in + (int64_t)t * R * 2 * H, bytes, bar);
   };
-  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  if (tid == 0 && t < zt.ntiles) issue(t);
   RowWork<Z::PSH> wk{work, Z::LDW};
   float2* nyq = main + zt.nyq_off;
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
-    const bool more = i + 1 < ntl;
+  for (int i = 0; t < zt.ntiles; ++i) {
     const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) {
       if (tid == 0 && err) atomicExch(err, 6);
@@ -123,9 +117,13 @@ zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* 
       return v;
     };
     auto rel = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue(t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < zt.ntiles) {
+          fence_proxy_async_smem();
+          issue(nt);
+        }
       }
     };
     p2_rows_to_work<Sch>(wk, in0, rel, tw, -1, tid, nthr);
@@ -149,6 +147,7 @@ zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* 
       else if (H - k != k) main[row * H + (H - k)] = xhk;
     }
     __syncthreads();
+    t = s_next;
   }
 }
 
@@ -161,7 +160,7 @@ struct SrcIdentity {
 template <class Sch>
 __global__ void __launch_bounds__(512)
 zc2r_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restrict__ twr, float* __restrict__ out,
-                 const float2* __restrict__ tw, int* err) {
+                 const float2* __restrict__ tw, int* err, int* tick) {
   using Z = ZShape<Sch>;
   constexpr int H = Z::H;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -173,18 +172,17 @@ zc2r_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restric
   const int tid = threadIdx.x, nthr = blockDim.x;
   if (tid == 0) { mbar_init(bar, 1); mbar_fence_init(); }
   __syncthreads();
-  const int ntl = z_my_tiles(zt.ntiles);
+  __shared__ int s_next;
+  int t = blockIdx.x;
   auto issue = [&](int t) {
     const uint32_t b0 = (uint32_t)R * H * 8u, b1 = (uint32_t)R * 8u;
     mbar_arrive_expect_tx(bar, b0 + b1);
     bulk_load_1d(slot, V + (int64_t)t * R * H, b0, bar);
     bulk_load_1d(nq, V + zt.nyq_off + (int64_t)t * R, b1, bar);
   };
-  if (tid == 0 && ntl > 0) issue(blockIdx.x);
+  if (tid == 0 && t < zt.ntiles) issue(t);
   RowWork<Z::PSH> wk{work, Z::LDW};
-  for (int i = 0; i < ntl; ++i) {
-    const int t = blockIdx.x + i * gridDim.x;
-    const bool more = i + 1 < ntl;
+  for (int i = 0; t < zt.ntiles; ++i) {
     const bool ok = mbar_wait_bounded(bar, (uint32_t)(i & 1));
     if (!__syncthreads_and(ok)) {
       if (tid == 0 && err) atomicExch(err, 10);
@@ -192,9 +190,13 @@ zc2r_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restric
     }
     auto in0 = [&](int c, int k) { return c2r_pack_tile(slot, nq, H, c, k, twr); };
     auto rel = [&]() {
-      if (tid == 0 && more) {
-        fence_proxy_async_smem();
-        issue(t + gridDim.x);
+      if (tid == 0) {
+        const int nt = next_tile(tick, t);
+        s_next = nt;
+        if (nt < zt.ntiles) {
+          fence_proxy_async_smem();
+          issue(nt);
+        }
       }
     };
     p2_rows_to_work<Sch>(wk, in0, rel, tw, +1, tid, nthr);
@@ -205,6 +207,7 @@ zc2r_pipe_kernel(const float2* __restrict__ V, ZTile zt, const float2* __restric
       o[f] = wk.at(r, m);
     }
     __syncthreads();
+    t = s_next;
   }
 }
 

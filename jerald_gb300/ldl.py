@@ -55,7 +55,7 @@ class FusedLDL:
     def __init__(self, nmesh, box, nparts: int, nstep: int = 2, kind: str = "sm", L1=None,
                  grad_mode: str = "reference", paint_method: str = "atomic", device="cuda",
                  pipelined: bool = True, recompute: bool = False, n: float = 0.0, index: float = 1.0,
-                 starmap=None):
+                 starmap=None, x_radix: int = 8, min_cols: int = 0, bin_tile: int = 16):
         nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
         self.nmesh = tuple(int(v) for v in nm)
         self.box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float32).reshape(-1), (3,)))
@@ -79,6 +79,13 @@ class FusedLDL:
         self.paint_method = paint_method
         self.pipelined = bool(pipelined)
         self.recompute = bool(recompute)
+        # schedule choices (the same step, different speed): radix of the x
+        # passes' schedules where radix-8 ones fit (8 or 16), narrowest
+        # pipelined tile (0 = automatic, 4, 8 or 16 columns), binning tile
+        # edge of the "tiled" paint (16, 8 or 20 cells)
+        if x_radix not in (8, 16) or min_cols not in (0, 4, 8, 16) or bin_tile not in (16, 8, 20):
+            raise ValueError("x_radix must be 8 or 16, min_cols 0, 4, 8 or 16, bin_tile 16, 8 or 20")
+        self.x_radix, self.min_cols, self.bin_tile = int(x_radix), int(min_cols), int(bin_tile)
         self.nparts = int(nparts)
         self.nstep = int(nstep)
         self.nparams = {"sm": 5 * self.nstep + 3, "dm": 5 * self.nstep, "HI": 10 * self.nstep + 12}[kind]
@@ -105,7 +112,10 @@ class FusedLDL:
     @property
     def options(self) -> int:
         """Option bits of jld_ldl_step_f32."""
-        return _PAINT[self.paint_method] | (0 if self.pipelined else 2) | (8 if self.recompute else 0)
+        cols = {0: 0, 4: 1, 8: 2, 16: 3}[self.min_cols] << 5
+        tile = {16: 0, 8: 1, 20: 2}[self.bin_tile] << 7
+        return (_PAINT[self.paint_method] | (0 if self.pipelined else 2) | (8 if self.recompute else 0)
+                | (16 if self.x_radix == 16 else 0) | cols | tile)
 
     @property
     def workspace_bytes(self) -> int:
@@ -235,7 +245,7 @@ class HostFeed:
     amount.
     """
 
-    def __init__(self, step: FusedLDL, mask=None, copy: str = "kernel", ctas: int = 16):
+    def __init__(self, step: FusedLDL, mask=None, copy: str = "kernel", ctas: int = 4):
         if copy not in ("kernel", "engine"):
             raise ValueError("copy must be 'kernel' or 'engine'")
         self.step = step
