@@ -530,7 +530,10 @@ def run_precision(args):
     """Precision study on the benchmark workload: the fused FP32 step and the
     plain FP32 primitives against the FP64 oracle (the CPU restatement of the
     reference's pipeline) on the same positions and target; L1 loss in both
-    gradient conventions and L2 loss.  Prints one JSON object."""
+    gradient conventions and L2 loss.  The fused step is also compared with
+    the FP64 oracle that keeps positions in float32 between layers
+    (`*_vs_f32pos`), which separates the error of storing positions in
+    float32 from the kernels' own.  Prints one JSON object."""
     import torch
     import __graft_entry__
     __graft_entry__.build()
@@ -579,6 +582,11 @@ def run_precision(args):
             res[key]["near_tie_pixels"] = ties
             res[key]["b_grad_tie_bound"] = 2.0 * ties / diff.size
         del o
+        o = oldl.LDLOracle((n,) * 3, box, kind="sm", L1=L1, pos_dtype=np.float32)
+        l64f = o.forward(params, X, tgt_h, nstep)
+        g64f = {m: o.backward(m) for m in ("reference", "true")}
+        res[key]["loss_f64_f32pos"] = l64f
+        del o
         for mode in ("reference", "true"):
             step = FusedLDL(n, box, pos.shape[0], nstep=nstep, kind="sm", L1=L1, grad_mode=mode, device=dev)
             l32, g32 = step(pos, params, target)
@@ -586,6 +594,8 @@ def run_precision(args):
             del step
             torch.cuda.empty_cache()
             res[key][f"fused_{mode}"] = {"loss_rel_err": abs(l32 - l64) / abs(l64), **compare(g32, g64[mode])}
+            res[key][f"fused_{mode}_vs_f32pos"] = {"loss_rel_err": abs(l32 - l64f) / abs(l64f),
+                                                   **compare(g32, g64f[mode])}
         if L1:
             pm = PMesh(n, box, device=dev, dtype=torch.float32)
             model = JERALDModel(pos, target, pm, Nstep=nstep, kind="sm")

@@ -81,11 +81,12 @@ def save_tuning(path: str) -> None:
 
 
 def autotune(nmesh, box, pos, target, params, nstep=2, kind="sm", L1=None, grad_mode="reference",
-             candidates=None, reps: int = 3, device="cuda") -> dict:
+             candidates=None, reps: int = 5, device="cuda") -> dict:
     """Fastest configuration of the fused step for this box shape and
-    clustering level (cached).  Each candidate runs one untimed and `reps`
-    timed eager steps; the candidates must agree on the loss (they compute
-    the same step).  `candidates` replaces the staged search by one list."""
+    clustering level (cached).  Each candidate is captured into a CUDA graph
+    and timed over `reps` replays after one untimed replay; the candidates
+    must agree on the loss (they compute the same step).  `candidates`
+    replaces the staged search by one list."""
     nm = np.broadcast_to(np.asarray(nmesh, dtype=np.int64).reshape(-1), (3,))
     level = clustering_level(pos, nm, box)
     key = _key(nm, pos.shape[0], kind, nstep, level)
@@ -99,17 +100,21 @@ def autotune(nmesh, box, pos, target, params, nstep=2, kind="sm", L1=None, grad_
             return times[name]
         step = FusedLDL(nm, box, pos.shape[0], nstep=nstep, kind=kind, L1=L1, grad_mode=grad_mode,
                         device=device, **cand)
-        step(pos, params, target)
+        # timed as the batch runs it: replays of a captured graph (eager
+        # calls of a small box measure the host's launch work instead)
+        step._set_params(params)
+        g = step.capture_graph(pos, target)
+        g.replay()
         torch.cuda.synchronize(device)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            loss, _ = step(pos, params, target)
+            g.replay()
         e1.record()
         torch.cuda.synchronize(device)
         times[name] = e0.elapsed_time(e1) / reps
-        losses.append(float(loss))
-        del step
+        losses.append(float(step.out[0]))
+        del g, step
         return times[name]
 
     def best_of(cands):

@@ -107,11 +107,20 @@ def fftfreq_signed(n: int) -> np.ndarray:
 
 @dataclass
 class LDLOracle:
+    """FP64 forward and adjoint of the LDL model (kinds "sm" and "dm").
+
+    pos_dtype=np.float32 rounds the positions after every layer to float32
+    (then computes on in FP64): the storage of an FP32 pipeline, which keeps
+    each layer's particle positions in float32 as the reference's FP32 path
+    does.  A displacement smaller than half a float32 ulp of the coordinate
+    is then partly lost, an error no FP32 kernel arithmetic can avoid; this
+    oracle separates it from the kernels' own."""
     nmesh: tuple
     box: tuple
     kind: str = "sm"
     L1: bool = True
     cache: dict = field(default_factory=dict)
+    pos_dtype: object = np.float64
 
     def __post_init__(self):
         self.nmesh = tuple(int(v) for v in np.broadcast_to(np.asarray(self.nmesh), (3,)))
@@ -191,6 +200,8 @@ class LDLOracle:
         layers = []
         for l in range(nstep):
             X, c = self.layer_forward(X, params[5 * l: 5 * l + 5], fact)
+            if self.pos_dtype != np.float64:
+                X = X.astype(self.pos_dtype).astype(np.float64)
             layers.append(c)
         if self.kind == "dm":
             mu = w = b = 0.0

@@ -88,8 +88,12 @@ def test_schedule_options_give_the_same_step(cfg):
 
 def test_batch_mixed_radix_boxes_match_fp64_oracle():
     """Boxes of 96^3 and 192^3 (mixed radix: generic FFT passes) in one
-    batch graph, each against the FP64 oracle: loss within 1e-5, gradient
-    within 1e-3 norm-wise."""
+    batch graph, each against the FP64 oracle that keeps the positions in
+    float32 between layers as the FP32 step does: loss within 1e-6,
+    gradient within 1e-4 norm-wise; and against the plain FP64 oracle within
+    5e-5 and 1e-3 (at 192^3, a 300-unit box, the layers' displacements of
+    ~4e-5 units are about one float32 ulp of the coordinates, and their
+    rounding alone moves the FP64 loss by 1.4e-5)."""
     import os
     from jerald_gb300 import synth
     from jerald_gb300.batch import Box, FusedLDLBatch
@@ -116,9 +120,14 @@ def test_batch_mixed_radix_boxes_match_fp64_oracle():
         torch.cuda.synchronize()
         for b, p, X, (lb, gb) in zip(boxes, params, X64, res):
             n = int(b.nmesh)
+            tgt = b.target.cpu().numpy().astype(np.float64)
+            o = oldl.LDLOracle((n,) * 3, b.box, kind="sm", L1=True, pos_dtype=np.float32)
+            lo, go = o.loss_and_grad(p, X, tgt, 2, mode="reference")
+            assert abs(lb - lo) <= 1e-6 * abs(lo)
+            assert np.linalg.norm(gb - go) / np.linalg.norm(go) < 1e-4
             o = oldl.LDLOracle((n,) * 3, b.box, kind="sm", L1=True)
-            lo, go = o.loss_and_grad(p, X, b.target.cpu().numpy().astype(np.float64), 2, mode="reference")
-            assert abs(lb - lo) <= 1e-5 * abs(lo)
+            lo, go = o.loss_and_grad(p, X, tgt, 2, mode="reference")
+            assert abs(lb - lo) <= 5e-5 * abs(lo)
             assert np.linalg.norm(gb - go) / np.linalg.norm(go) < 1e-3
     finally:
         offt.set_workers(1)

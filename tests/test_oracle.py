@@ -214,3 +214,24 @@ def test_model_loss_smoothing_known_answer():
         assert abs(lv - (c * K0) ** 2) <= 1e-9 * (c * K0) ** 2
     l0, _ = model_loss((n,) * 3, box, "dm", p, X, tgt, 2, n=0, L1=True)
     assert abs(l0 - c) <= 1e-12
+
+
+def test_oracle_float32_position_storage():
+    """pos_dtype=np.float32 keeps every layer's positions float32-representable
+    and otherwise computes the same pipeline: at 16^3 its loss and gradient
+    stay within 1e-6 of the FP64 oracle's."""
+    from jerald_gb300 import synth
+    from oracle import ldl as oldl
+    n, L = 16, 25.0
+    X = synth.zeldovich(n, L, 0.5, seed=1, dtype=np.float32).astype(np.float64)
+    p = synth.default_params(2)
+    t = synth.lognormal_noise((n,) * 3, 0.1, 2)
+    a = oldl.LDLOracle((n,) * 3, L)
+    b = oldl.LDLOracle((n,) * 3, L, pos_dtype=np.float32)
+    la, lb = a.forward(p, X, t, 2), b.forward(p, X, t, 2)
+    xf = b.cache["X_final"]
+    assert np.array_equal(xf, xf.astype(np.float32).astype(np.float64))
+    assert not np.array_equal(a.cache["X_final"], a.cache["X_final"].astype(np.float32).astype(np.float64))
+    assert abs(la - lb) <= 1e-6 * abs(la)
+    ga, gb = a.backward(), b.backward()
+    assert np.abs(ga - gb).max() <= 1e-6 * np.abs(ga).max()
