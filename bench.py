@@ -326,7 +326,8 @@ def run_profile(args):
     params = synth.default_params(2)
     pos, box = make_workload(n, dev, seed=0)
     target = torch.ones((n, n, n), device=dev)
-    step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, paint_method=args.paint, device=dev)
+    step = FusedLDL(n, box, pos.shape[0], nstep=2, kind="sm", L1=True, paint_method=args.paint, device=dev,
+                    x_radix=args.x_radix, min_cols=args.min_cols)
     for _ in range(args.warmup + args.steps):
         step(pos, params, target)
     torch.cuda.synchronize()
@@ -623,6 +624,10 @@ def main():
     ap.add_argument("--precision", action="store_true",
                     help="compare the fused FP32 step with the FP64 primitive pipeline on the workload")
     ap.add_argument("--paint", default="atomic", choices=["atomic", "warp", "tiled"])
+    ap.add_argument("--x-radix", type=int, default=8, choices=[8, 16],
+                    help="x passes' schedule radix where radix-8 ones fit")
+    ap.add_argument("--min-cols", type=int, default=0, choices=[0, 4, 8, 16],
+                    help="narrowest pipelined tile (0: automatic)")
     ap.add_argument("--nstep", type=int, default=2, help="displacement layers")
     ap.add_argument("--batch", type=int, default=0,
                     help="instead of the main workload: N boxes of mixed meshes in one graph (prints its own line)")
@@ -672,7 +677,7 @@ def main():
     target = make_target(pos, n, box, params, dev, nstep)
     N = pos.shape[0]
     step = FusedLDL(n, box, N, nstep=nstep, kind="sm", L1=True, grad_mode="reference", paint_method=args.paint,
-                    device=dev, recompute=args.recompute)
+                    device=dev, recompute=args.recompute, x_radix=args.x_radix, min_cols=args.min_cols)
     step(pos, params, target)
     step.capture(pos, target)
     launches_per_step = step.graph_kernels()

@@ -456,9 +456,10 @@ static int ldl_step(const StepArgs& a) {
       if ((s = xmap(&mA, W[0], px1))) return s;
       s = with_x([&](auto sch) {
         using Sch = decltype(sch);
-        int r = ensure_smem(xfilt_pipe_kernel<Sch>, px1.smem);
+        auto kern = hi ? xfilt_pipe_kernel<Sch, true> : xfilt_pipe_kernel<Sch, false>;
+        int r = ensure_smem(kern, px1.smem);
         if (r) return r;
-        xfilt_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(mA, px1.g, kt, prm, a.kind, scale, S_l, W[1],
+        kern<<<px1.grid, px1.nthr, px1.smem, st>>>(mA, px1.g, kt, prm, a.kind, scale, S_l, W[1],
                                                                     W[2], pl.px.tw, err, S2_l, tick());
         return 0;
       });
@@ -715,9 +716,10 @@ static int ldl_step(const StepArgs& a) {
       if ((s = xmap(&m0, W[0], px1)) || (s = xmap(&m1, W[3], px1)) || (s = xmap(&m2, S_l, px1))) return s;
       s = with_x([&](auto sch) {
         using Sch = decltype(sch);
-        int r = ensure_smem(xbwd_pipe_kernel<Sch>, px1.smem);
+        auto kern = hi ? xbwd_pipe_kernel<Sch, true> : xbwd_pipe_kernel<Sch, false>;
+        int r = ensure_smem(kern, px1.smem);
         if (r) return r;
-        xbwd_pipe_kernel<Sch><<<px1.grid, px1.nthr, px1.smem, st>>>(m0, m1, m2, px1.g, kt, prm, a.kind, a.mode,
+        kern<<<px1.grid, px1.nthr, px1.smem, st>>>(m0, m1, m2, px1.g, kt, prm, a.kind, a.mode,
                                                                    scale, W[1], part, pl.px.tw, err,
                                                                    hi ? W[2] : nullptr, tick());
         return 0;

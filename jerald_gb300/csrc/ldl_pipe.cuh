@@ -20,7 +20,7 @@ __device__ __forceinline__ void xcols(const SGeom& g, int t, int* ky, int* kz, i
 
 // Forward x pass: S = FFT_x(A) (kept for the adjoint), P = 1e-2 alpha G S / Nc,
 // T0 = iFFT_x(P), T1 = iFFT_x(-i c_x P).
-template <class Sch>
+template <class Sch, bool HI = false>
 __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, const float* __restrict__ params,
                   int kind, float scale, float2* __restrict__ S, float2* __restrict__ T0,
@@ -66,7 +66,7 @@ xfilt_pipe_kernel(const __grid_constant__ CUtensorMap mA, SGeom g, KTables kt, c
       const float m = a * gr.g;
       float2 v = ac.at(c, j);
       float2 p = make_float2(v.x * m, v.y * m);
-      if (S2) hi_add_src2(p, S2[base + c + (int64_t)j * g.es], params, scale, __ldg(kt.kx + j),
+      if (HI) hi_add_src2(p, S2[base + c + (int64_t)j * g.es], params, scale, __ldg(kt.kx + j),
                           __ldg(kt.ky + cky[c]), __ldg(kt.kz + ckz[c]));
       ac.at(c, j) = p;
     }
@@ -204,7 +204,7 @@ yfwd_comb_pipe_kernel(const __grid_constant__ CUtensorMap mAx, const __grid_cons
 
 // Adjoint x pass with the parameter-gradient reductions; items per tile:
 // Bx, D, S.  Partials per block: [d alpha, d kh, d kl, d nu].
-template <class Sch>
+template <class Sch, bool HI = false>
 __global__ void __launch_bounds__(512, Sch::E == 8 ? 2 : 1)
 xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant__ CUtensorMap mD,
                  const __grid_constant__ CUtensorMap mS, SGeom g, KTables kt, const float* __restrict__ params,
@@ -260,7 +260,7 @@ xbwd_pipe_kernel(const __grid_constant__ CUtensorMap mBx, const __grid_constant_
       const int c = f & (g.cols - 1), j = f >> g.cshift;
       const int kz = ckz[c];
       const float2 W = ac.at(c, j);
-      if (Wout) Wout[base + c + (int64_t)j * g.es] = W;
+      if (HI) Wout[base + c + (int64_t)j * g.es] = W;
       const float2 Sv = slot[j * g.cols + c];
       Green gr = green_fn(__ldg(kt.kx + j), __ldg(kt.ky + cky[c]), __ldg(kt.kz + kz), kind, kh, kl, nu);
       const float reWS = W.x * Sv.x + W.y * Sv.y;
