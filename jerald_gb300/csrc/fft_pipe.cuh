@@ -1,4 +1,4 @@
-// Pipelined pencil-FFT passes for power-of-two line lengths (sm_103a).
+// Pipelined pencil-FFT passes for line lengths 2^k and 3 x 2^k (sm_103a).
 //
 // Persistent CTAs walk a stream of "items" (one input tile each).  A ring of
 // shared-memory staging slots is filled by the Tensor Memory Accelerator:
@@ -102,12 +102,14 @@ __device__ __forceinline__ void bulk_load_1d(void* dst, const void* src, uint32_
 }
 
 // ---------------------------------------------------------------------------
-// Compile-time power-of-two schedules (radix of the first stage first).
-constexpr int cmax_pack(int a) { return a; }
+// Compile-time radix schedules (radix of the first stage first): powers of
+// two, and 3 x a power of two with one radix-3 stage last.
+constexpr int cgcd(int a, int b) { return b == 0 ? a : cgcd(b, a % b); }
+constexpr int clcm_pack(int a) { return a; }
 template <class... Ts>
-constexpr int cmax_pack(int a, Ts... r) {
-  int b = cmax_pack(r...);
-  return a > b ? a : b;
+constexpr int clcm_pack(int a, Ts... r) {
+  const int b = clcm_pack(r...);
+  return a / cgcd(a, b) * b;
 }
 constexpr int clog2(int v) {
   int s = 0;
@@ -120,7 +122,9 @@ struct P2 {
   static constexpr int nst = sizeof...(Rs);
   static constexpr int rad[nst] = {Rs...};
   static constexpr int n = (1 * ... * Rs);
-  static constexpr int E = cmax_pack(Rs...);
+  // values per thread per line: a multiple of every radix (the largest
+  // radix for a power-of-two schedule)
+  static constexpr int E = clcm_pack(Rs...);
   static constexpr int pre(int s) {
     int p = 1;
     for (int i = 0; i < s; ++i) p *= rad[i];
@@ -156,7 +160,6 @@ __device__ __forceinline__ void p2_stage(const Ld& ld, const St& st, const float
   constexpr int T = N / R;
   constexpr int Q = Sch::E / R;
   constexpr int TWS = N / (P * R);
-  constexpr int LT = clog2(T);
   float2 u[Q][R];
   int cc[Q], bb[Q];
 #pragma unroll
@@ -167,8 +170,10 @@ __device__ __forceinline__ void p2_stage(const Ld& ld, const St& st, const float
       c = id & ((1 << cshift) - 1);
       b = id >> cshift;
     } else {
-      b = id & (T - 1);
-      c = id >> LT;
+      // unsigned division by constants: shifts and masks when T is a power
+      // of two
+      b = (int)((unsigned)id % (unsigned)T);
+      c = (int)((unsigned)id / (unsigned)T);
     }
     cc[q] = c;
     bb[q] = b;
@@ -182,6 +187,7 @@ __device__ __forceinline__ void p2_stage(const Ld& ld, const St& st, const float
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int b = bb[q], c = cc[q];
+    static_assert((P & (P - 1)) == 0, "only the last stage of a schedule may have a radix other than 2^k");
     const int k = b & (P - 1);
     if constexpr (P > 1) {
       if (k != 0) {
@@ -250,6 +256,13 @@ template <> struct P2For<256> { using type = P2<16, 16>; };
 template <> struct P2For<512> { using type = P2<16, 16, 2>; };
 template <> struct P2For<1024> { using type = P2<16, 16, 4>; };
 template <> struct P2For<2048> { using type = P2<16, 16, 8>; };
+// 3 x 2^k (meshes of 96 and 192 cells per axis and their half lengths): the
+// radix-4 and radix-2 stages first, one radix-3 stage last, E = 12 values
+// per thread per line (the lcm of the radices; radix-8 stages would make it
+// 24 and spill in the kernels capped at 64-96 registers).
+template <> struct P2For<48> { using type = P2<4, 4, 3>; };
+template <> struct P2For<96> { using type = P2<4, 4, 2, 3>; };
+template <> struct P2For<192> { using type = P2<4, 4, 4, 3>; };
 
 // Radix-8 family: 8 values per thread per line, so a kernel can stay under
 // 64 registers and keep twice the warps resident (used by the x passes,
@@ -279,11 +292,14 @@ inline int with_p2_8(int n, F&& body) {
   }
 }
 
-// Calls body(P2For<N>::type{}) for a supported power of two; returns -1 if
-// n has no pipelined schedule.
+// Calls body(P2For<N>::type{}) for a supported length (a power of two from
+// 16 to 2048, or 48, 96, 192); returns -1 if n has no pipelined schedule.
 template <class F>
 inline int with_p2(int n, F&& body) {
   switch (n) {
+    case 48: return body(P2For<48>::type{});
+    case 96: return body(P2For<96>::type{});
+    case 192: return body(P2For<192>::type{});
     case 16: return body(P2For<16>::type{});
     case 32: return body(P2For<32>::type{});
     case 64: return body(P2For<64>::type{});
@@ -294,6 +310,17 @@ inline int with_p2(int n, F&& body) {
     case 2048: return body(P2For<2048>::type{});
     default: return -1;
   }
+}
+
+// Values per thread per line (E) and first-stage shift (PSH of the row
+// work buffer) of the P2For schedule of length n; false if there is none.
+inline bool p2_shape(int n, int* E, int* psh) {
+  return with_p2(n, [&](auto sch) {
+           using Sch = decltype(sch);
+           *E = Sch::E;
+           *psh = clog2(Sch::rad[0]);
+           return 0;
+         }) == 0;
 }
 
 }  // namespace jld

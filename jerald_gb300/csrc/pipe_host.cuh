@@ -77,7 +77,13 @@ struct PipeGeom {
 inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, int regs = 128, int min_cols_req = 0) {
   PipeGeom p;
   const int lines = ax == 1 ? ny : nx;
-  if (lines < 16 || lines > 2048 || (lines & (lines - 1)) || h < 2 || (h & 1)) return p;
+  if (lines < 16 || lines > 2048 || h < 2 || (h & 1)) return p;
+  if (lines & (lines - 1)) {
+    // 3 x 2^k: only the P2For family has such schedules; lines of at most
+    // 256 keep a tile one TMA box high
+    int psh = 0;
+    if (E != 16 || lines > 256 || !p2_shape(lines, &E, &psh)) return p;
+  }
   // Widest tile (<= 16 columns, <= 512 threads, cols dividing h) whose CTA
   // leaves room for a second one on the SM (a CTA waits at barriers between
   // FFT stages; a second CTA keeps the SM busy meanwhile), else the widest
@@ -124,7 +130,8 @@ inline PipeGeom pipe_geom(int nx, int ny, int h, int ax, int nacc, int E = 16, i
 }
 
 // Geometry of a pipelined z pass over `nin` meshes (tiles of R whole rows of
-// each), or ok = false when h is not a power of two in [16, 2048] or no even
+// each), or ok = false when h has no pipelined schedule (2^k in [16, 2048],
+// 48, 96, 192) or no even
 // R divides the row count within 512 threads and ~110 KB of shared memory
 // (two CTAs per SM).
 struct ZPipeGeom {
@@ -141,11 +148,12 @@ struct ZPipeGeom {
 inline ZPipeGeom zpipe_geom(int64_t rows, int h, int nin, size_t slot_row, size_t cap = 110 * 1024,
                             int max_thr = 512) {
   ZPipeGeom z;
-  if (h < 16 || h > 2048 || (h & (h - 1))) return z;
-  const int ldw = h + h / 16;
+  int E = 0, psh = 0;
+  if (h < 16 || h > 2048 || !p2_shape(h, &E, &psh)) return z;
+  const int ldw = h + (h >> psh);  // ZShape<P2For<h>>::LDW
   for (int R = 32; R >= 2; R >>= 1) {
     const int lines = nin * R;
-    const int64_t thr = (int64_t)lines * h / 16;
+    const int64_t thr = (int64_t)lines * h / E;
     const size_t smem = (size_t)R * slot_row + (size_t)lines * ldw * 8 + 16;
     if (thr > max_thr || rows % R || smem > cap) continue;
     if (thr < 32) return z;

@@ -218,8 +218,8 @@ zr2c3_pipe_kernel(const float4* __restrict__ gb4, ZTile zt, const float2* __rest
       const int c = f / HH, k = f - c * HH;
       const int d = c / R, r = c - d * R;
       const int64_t row = row0 + r;
-      const float2 z = wk.at(c, k & (H - 1));
-      const float2 zm = wk.at(c, (H - k) & (H - 1));
+      const float2 z = wk.at(c, k);  // k <= H/2 < H
+      const float2 zm = wk.at(c, k == 0 ? 0 : H - k);
       const float2 zc = make_float2(zm.x, -zm.y);
       const float2 xe = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
       const float2 dd = make_float2(0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y));

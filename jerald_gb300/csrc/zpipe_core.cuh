@@ -133,8 +133,8 @@ zr2c_pipe_kernel(const float* __restrict__ in, Src src, ZTile zt, const float2* 
     for (int f = tid; f < R * HH; f += nthr) {
       const int c = f / HH, k = f - c * HH;
       const int64_t row = row0 + c;
-      const float2 z = wk.at(c, k & (H - 1));
-      const float2 zm = wk.at(c, (H - k) & (H - 1));
+      const float2 z = wk.at(c, k);  // k <= H/2 < H
+      const float2 zm = wk.at(c, k == 0 ? 0 : H - k);
       const float2 zc = make_float2(zm.x, -zm.y);
       const float2 xe = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
       const float2 dd = make_float2(0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y));

@@ -175,7 +175,7 @@ def test_fused_graph_replay_matches_eager(paint):
     assert abs(float(l2) - float(l0)) > 1e-6 * abs(float(l0))
 
 
-@pytest.mark.parametrize("n", [32, 64, 128])
+@pytest.mark.parametrize("n", [32, 64, 96, 128, 192])
 def test_pipelined_passes_match_generic_passes(n):
     # L2 loss: with L1, rounding-level differences between two valid FP32
     # forward paths flip sign(F - t) in a few cells and move d/db visibly
@@ -196,7 +196,8 @@ def test_pipelined_passes_match_generic_passes(n):
     assert float((xa - xb).abs().max()) < 1e-4
 
 
-@pytest.mark.parametrize("nm", [(512, 16, 32), (16, 512, 64), (64, 32, 1024), (1024, 16, 32)])
+@pytest.mark.parametrize("nm", [(512, 16, 32), (16, 512, 64), (64, 32, 1024), (1024, 16, 32), (96, 192, 48),
+                                (192, 96, 96), (48, 64, 384)])
 def test_pipelined_passes_match_generic_non_cubic(nm):
     # long x / y / z lines: narrower pipelined tiles (two CTAs per SM) and
     # few rows per z tile

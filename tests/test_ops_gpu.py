@@ -281,7 +281,8 @@ def test_error_statuses(jl):
 
 FFT_SHAPES = [(8, 8, 8), (16, 16, 16), (20, 20, 20), (12, 10, 8), (32, 48, 40), (64, 64, 64),
               (96, 96, 96), (2, 3, 2), (1, 1, 2), (128, 128, 128), (256, 64, 512), (30, 30, 30),
-              (16, 256, 256), (16, 512, 512), (192, 192, 192), (160, 96, 144)]
+              (16, 256, 256), (16, 512, 512), (192, 192, 192), (160, 96, 144), (96, 192, 96),
+              (192, 48, 384)]
 
 
 def _ws(jl, nm, dt):
