@@ -187,6 +187,9 @@ def time_primitives(pos, n, box, steps, warmup):
     ops = {
         "paint": (lambda: _lib.call("jld_ppaint_box_f32", sp, P(pos), N, None, ct.c_float(1.0), n, n, n, bp, P(mesh)),
                   12 * N + 4 * C),
+        # warp-aggregated atomics (lanes on one cell merged first)
+        "paint_warp": (lambda: _lib.call("jld_ppaint_box_method_f32", sp, P(pos), N, None, ct.c_float(1.0), n, n, n,
+                                         bp, 1, P(mesh)), 12 * N + 4 * C),
         # stable sort by cell key (keys and order written: 12N in, 8N out)
         "cell_sort": (lambda: _lib.call("jld_cell_sort_f32", sp, P(pos), N, n, n, n, bp, P(keys), P(order), P(cws),
                                         cws.numel()), 20 * N),
