@@ -167,79 +167,98 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
       load_pos<T, BOX>(src, p, q);
       m = mass ? __ldg(mass + p) : mscalar;
     }
-    Corners<T> c;
-    cic_corners(q, g, c);
-    T lo[3], hi[3];
+    // Batches whose 32 particles all lie inside the mesh (nearly all) take a
+    // path without the per-corner validity flags that the reference's
+    // out-of-range semantics need (the paint is issue-bound).
+    bool inr_lane = live;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
-    T w[8];
+    for (int a = 0; a < 3; ++a) inr_lane = inr_lane && (unsigned)(int)q[a] < (unsigned)nax[a];
+    auto scatter = [&](auto fast_tag) {
+      constexpr bool FAST = decltype(fast_tag)::value;
+      const bool lv = FAST || live;
+      Corners<T> c;
+      if constexpr (FAST) cic_corners_inrange(q, g, c);
+      else cic_corners(q, g, c);
+      T lo[3], hi[3];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      int bits = corner_axis_bits(k);
-      if constexpr (UNIT) w[k] = corner_ok(c, bits) ? corner_weight(lo, hi, bits) : T(0);
-      else w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
-    }
-    // z span first: lattice-ordered batches (32 cells along z) leave here
-    {
-      unsigned mn[3], mx[3];
-      int ii[3];
-      bool clump = false;
-      ii[2] = (int)q[2];
-      mn[2] = __reduce_min_sync(full, live ? (unsigned)ii[2] : 0xffffffffu);
-      mx[2] = __reduce_max_sync(full, live ? (unsigned)ii[2] : 0u);
-      if (mx[2] - mn[2] <= 2u) {
-        ii[0] = (int)q[0];
-        ii[1] = (int)q[1];
-        bool inr = true;
+      for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = sub_rn(T(1), c.d[a]); }
+      T w[8];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) inr = inr && (unsigned)ii[a] < (unsigned)nax[a];
-#pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          mn[a] = __reduce_min_sync(full, live ? (unsigned)ii[a] : 0xffffffffu);
-          mx[a] = __reduce_max_sync(full, live ? (unsigned)ii[a] : 0u);
-        }
-        clump = __all_sync(full, inr || !live) && mx[0] - mn[0] <= 2u && mx[1] - mn[1] <= 2u;
+      for (int k = 0; k < 8; ++k) {
+        const int bits = corner_axis_bits(k);
+        if constexpr (FAST && UNIT) w[k] = corner_weight(lo, hi, bits);
+        else if constexpr (FAST) w[k] = mul_rn(corner_weight(lo, hi, bits), m);
+        else if constexpr (UNIT) w[k] = corner_ok(c, bits) ? corner_weight(lo, hi, bits) : T(0);
+        else w[k] = mul_rn(mul_rn(corner_weight(lo, hi, bits), m), corner_ok(c, bits) ? T(1) : T(0));
       }
-      if (clump) {
-        win[lane] = T(0);
-        win[lane + 32] = T(0);
-        __syncwarp();
-        if (live) {
-          const int wb = ((ii[0] - (int)mn[0]) * 4 + (ii[1] - (int)mn[1])) * 4 + (ii[2] - (int)mn[2]);
+      // z span first: lattice-ordered batches (32 cells along z) leave here
+      {
+        unsigned mn[3], mx[3];
+        int ii[3];
+        bool clump = false;
+        ii[2] = (int)q[2];
+        mn[2] = __reduce_min_sync(full, lv ? (unsigned)ii[2] : 0xffffffffu);
+        mx[2] = __reduce_max_sync(full, lv ? (unsigned)ii[2] : 0u);
+        if (mx[2] - mn[2] <= 2u) {
+          ii[0] = (int)q[0];
+          ii[1] = (int)q[1];
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const int bits = corner_axis_bits(k);
-            atomicAdd(win + wb + (bits & 1) * 16 + ((bits >> 1) & 1) * 4 + (bits >> 2), w[k]);
+          for (int a = 0; a < 2; ++a) {
+            mn[a] = __reduce_min_sync(full, lv ? (unsigned)ii[a] : 0xffffffffu);
+            mx[a] = __reduce_max_sync(full, lv ? (unsigned)ii[a] : 0u);
           }
-        }
-        __syncwarp();
+          bool inr = FAST;
+          if constexpr (!FAST) {
+            inr = true;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int sl = lane + 32 * h;
-          const T v = win[sl];
-          if (v != T(0)) {
-            int gx = (int)mn[0] + (sl >> 4), gy = (int)mn[1] + ((sl >> 2) & 3), gz = (int)mn[2] + (sl & 3);
-            if (gx >= g.nx) gx -= g.nx;
-            if (gy >= g.ny) gy -= g.ny;
-            if (gz >= g.nz) gz -= g.nz;
-            atomicAdd(out + ((uint32_t)gx * (uint32_t)g.sx + (uint32_t)gy * (uint32_t)g.sy + (uint32_t)gz), v);
+            for (int a = 0; a < 3; ++a) inr = inr && (unsigned)ii[a] < (unsigned)nax[a];
+            inr = __all_sync(full, inr || !live);
           }
+          clump = inr && mx[0] - mn[0] <= 2u && mx[1] - mn[1] <= 2u;
         }
-        __syncwarp();
-        continue;
+        if (clump) {
+          win[lane] = T(0);
+          win[lane + 32] = T(0);
+          __syncwarp();
+          if (lv) {
+            const int wb = ((ii[0] - (int)mn[0]) * 4 + (ii[1] - (int)mn[1])) * 4 + (ii[2] - (int)mn[2]);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const int bits = corner_axis_bits(k);
+              atomicAdd(win + wb + (bits & 1) * 16 + ((bits >> 1) & 1) * 4 + (bits >> 2), w[k]);
+            }
+          }
+          __syncwarp();
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int sl = lane + 32 * h;
+            const T v = win[sl];
+            if (v != T(0)) {
+              int gx = (int)mn[0] + (sl >> 4), gy = (int)mn[1] + ((sl >> 2) & 3), gz = (int)mn[2] + (sl & 3);
+              if (gx >= g.nx) gx -= g.nx;
+              if (gy >= g.ny) gy -= g.ny;
+              if (gz >= g.nz) gz -= g.nz;
+              atomicAdd(out + ((uint32_t)gx * (uint32_t)g.sx + (uint32_t)gy * (uint32_t)g.sy + (uint32_t)gz), v);
+            }
+          }
+          __syncwarp();
+          return;
+        }
       }
-    }
-    const Pairing pr = zpair32_flags(live ? pair_key(c, g) : kNoPair);
+      const Pairing pr = zpair32_flags(lv ? pair_key(c, g) : kNoPair);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const T t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
-      if (pr.tz) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
-    }
-    if (live) {
+      for (int j = 0; j < 4; ++j) {
+        const T t = __shfl_up_sync(full, w[zpair_hi(j)], 1);
+        if (pr.tz) w[zpair_lo(j)] = add_rn(w[zpair_lo(j)], t);
+      }
+      if (lv) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if (pair_keeps(pr, k)) atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
-    }
+        for (int k = 0; k < 8; ++k)
+          if (pair_keeps(pr, k)) atomicAdd(out + corner_offset(c, corner_axis_bits(k), g), w[k]);
+      }
+    };
+    if (__all_sync(full, inr_lane)) scatter(std::true_type{});
+    else scatter(std::false_type{});
   }
 }
 

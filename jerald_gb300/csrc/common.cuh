@@ -235,6 +235,22 @@ __device__ __forceinline__ void cic_corners(const T p[3], const Grid3& g,
   }
 }
 
+// cic_corners for a point known to lie inside the mesh (0 <= int(p) < n on
+// every axis): the same offsets, every corner valid.
+template <typename T>
+__device__ __forceinline__ void cic_corners_inrange(const T p[3], const Grid3& g, Corners<T>& c) {
+  const int n[3] = {g.nx, g.ny, g.nz};
+  const uint32_t st[3] = {(uint32_t)g.sx, (uint32_t)g.sy, 1u};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int i = (int)p[a];
+    c.d[a] = sub_rn(p[a], (T)i);
+    c.o[a][0] = (uint32_t)i * st[a];
+    c.o[a][1] = (uint32_t)(i + 1 == n[a] ? 0 : i + 1) * st[a];
+    c.ok[a][0] = c.ok[a][1] = true;
+  }
+}
+
 // Flattened cell offset of corner q (0..7, reference order).
 __device__ __forceinline__ int corner_axis_bits(int q) {
   // bit a set => upper corner along axis a
