@@ -87,11 +87,14 @@ int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int
 constexpr int kTickRegions = 32, kTickStride = 32, kUnitBatches = 4;
 constexpr int kTicksPerLaunch = kTickRegions * kTickStride;
 struct WarpBatches {
-  int* tick;         // counters, or nullptr (grid-stride order)
+  int* tick;         // this warp's region counter, or nullptr (grid-stride order)
   int64_t unit_end;  // counters: end of the current unit
-  // Only these two stay live across a kernel's batch loop; the warp index,
+  int pending;       // counters, lane 0: the next unit's ticket, fetched a unit ahead
+  // Only these stay live across a kernel's batch loop; the warp index,
   // region and stride are recomputed when needed (registers are the scarce
-  // resource of the particle kernels).
+  // resource of the particle kernels).  The next ticket is fetched when a
+  // unit starts and read when it ends, so the atomic's round trip overlaps
+  // the unit's work (reading it at once cost the layer update 13 %).
   __device__ __forceinline__ static int64_t warps() { return (int64_t)gridDim.x * (blockDim.x >> 5); }
   __device__ __forceinline__ static int64_t warp() {
     return (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -99,27 +102,30 @@ struct WarpBatches {
   __device__ __forceinline__ static int64_t unit_start(int64_t region, int64_t q) {
     return (region + (int64_t)kTickRegions * q) * (32 * kUnitBatches);
   }
+  __device__ __forceinline__ void fetch() {
+    if ((threadIdx.x & 31) == 0) {
+      const int64_t region = warp() % kTickRegions;
+      const int wr = (int)((warps() - region + kTickRegions - 1) / kTickRegions);
+      pending = wr + atomicAdd(tick, 1);
+    }
+  }
   __device__ __forceinline__ int64_t first(int* tick_) {
-    tick = warps() >= kTickRegions ? tick_ : nullptr;
-    if (!tick) return 32 * warp();
     const int64_t w = warp();
+    tick = warps() >= kTickRegions ? tick_ + (w % kTickRegions) * kTickStride : nullptr;
+    if (!tick) return 32 * w;
     const int64_t b = unit_start(w % kTickRegions, w / kTickRegions);
     unit_end = b + 32 * kUnitBatches;
+    fetch();
     return b;
   }
   __device__ __forceinline__ int64_t next(int64_t base) {
     if (!tick) return base + 32 * warps();
     base += 32;
     if (base < unit_end) return base;
-    const int64_t region = warp() % kTickRegions;
-    int q = 0;
-    if ((threadIdx.x & 31) == 0) {
-      const int wr = (int)((warps() - region + kTickRegions - 1) / kTickRegions);
-      q = wr + atomicAdd(tick + region * kTickStride, 1);
-    }
-    q = __shfl_sync(0xffffffffu, q, 0);
-    const int64_t b = unit_start(region, q);
+    const int q = __shfl_sync(0xffffffffu, pending, 0);
+    const int64_t b = unit_start(warp() % kTickRegions, q);
     unit_end = b + 32 * kUnitBatches;
+    fetch();
     return b;
   }
 };
