@@ -349,7 +349,7 @@ def run_batch(args):
     from jerald_gb300.batch import FusedLDLBatch, make_c3_boxes
     dev = torch.device("cuda", 0)
     boxes, params = make_c3_boxes(seed=0, nbox=args.batch, device=dev)
-    b = FusedLDLBatch(boxes, streams=4, tune=True, device=dev)
+    b = FusedLDLBatch(boxes, streams=args.streams, tune=True, device=dev)
     b.capture()
     for _ in range(args.warmup):
         b.replay(params)
@@ -382,7 +382,7 @@ def run_batch(args):
                                   f"one particle per cell, 2 sm layers, one graph",
                       "ms_per_batch": ms, "boxes_per_s": len(boxes) * 1000.0 / ms,
                       "particle_steps_per_s": npart * 1000.0 / ms, "serial_graphs_ms": serial,
-                      "graph_kernels": b.graph_kernels(),
+                      "graph_kernels": b.graph_kernels(), "streams": args.streams,
                       "configs": [bx.config for bx in boxes]}), flush=True)
     return 0
 
@@ -634,6 +634,7 @@ def main():
     ap.add_argument("--nstep", type=int, default=2, help="displacement layers")
     ap.add_argument("--batch", type=int, default=0,
                     help="instead of the main workload: N boxes of mixed meshes in one graph (prints its own line)")
+    ap.add_argument("--streams", type=int, default=4, help="parallel graph branches of the --batch workload")
     ap.add_argument("--recompute", action="store_true",
                     help="memory plan: one force-mesh slot, recomputed in the adjoint")
     ap.add_argument("--snapmap", type=int, default=0,

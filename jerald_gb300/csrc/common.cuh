@@ -82,9 +82,9 @@ int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int
 // that start late (their SM partly held by other work: a host copy, another
 // box's step) take fewer units instead of holding the kernel up by a whole
 // share.  The regions keep the counters on separate cache lines.
-// Units of 4 batches: 29.40 ms per 512^3 step against 30.52 (2), 29.72 (8)
-// and 29.77 (16) on one box.
-constexpr int kTickRegions = 32, kTickStride = 32, kUnitBatches = 4;
+// Units of 16 batches: 29.07 ms per 512^3 step against 29.14 (8) and 29.27
+// (4) on one box; 1 and 2 were slower still (31.20, 29.74 on another).
+constexpr int kTickRegions = 32, kTickStride = 32, kUnitBatches = 16;
 constexpr int kTicksPerLaunch = kTickRegions * kTickStride;
 struct WarpBatches {
   int* tick;         // this warp's region counter, or nullptr (grid-stride order)
