@@ -117,7 +117,7 @@ paint_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ mass, T mscalar,
   const int nax[3] = {g.nx, g.ny, g.nz};
   // the staged copies run two batches ahead in the grid-stride order
   WarpBatches wb;
-  const int64_t base0 = wb.first(STAGED ? nullptr : tick);
+  const int64_t base0 = wb.first(STAGED ? nullptr : tick, n);
   const int64_t stride = 32 * WarpBatches::warps();
   auto issue = [&](int64_t b, int buf) {
     if (b + 32 <= n) {

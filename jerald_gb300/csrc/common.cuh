@@ -82,14 +82,15 @@ int paint_unit_f32(cudaStream_t st, const float* pos, int64_t n, int64_t nx, int
 // that start late (their SM partly held by other work: a host copy, another
 // box's step) take fewer units instead of holding the kernel up by a whole
 // share.  The regions keep the counters on separate cache lines.
-// Units of 16 batches: 29.07 ms per 512^3 step against 29.14 (8) and 29.27
-// (4) on one box; 1 and 2 were slower still (31.20, 29.74 on another).
+// Units of up to 16 batches: 29.07 ms per 512^3 step against 29.14 (8) and
+// 29.27 (4) on one box; 1 and 2 were slower still (31.20, 29.74 on another).
 constexpr int kTickRegions = 32, kTickStride = 32, kUnitBatches = 16;
 constexpr int kTicksPerLaunch = kTickRegions * kTickStride;
 struct WarpBatches {
   int* tick;         // this warp's region counter, or nullptr (grid-stride order)
   int64_t unit_end;  // counters: end of the current unit
   int pending;       // counters, lane 0: the next unit's ticket, fetched a unit ahead
+  int ub;            // counters: batches per unit
   // Only these stay live across a kernel's batch loop; the warp index,
   // region and stride are recomputed when needed (registers are the scarce
   // resource of the particle kernels).  The next ticket is fetched when a
@@ -99,8 +100,8 @@ struct WarpBatches {
   __device__ __forceinline__ static int64_t warp() {
     return (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   }
-  __device__ __forceinline__ static int64_t unit_start(int64_t region, int64_t q) {
-    return (region + (int64_t)kTickRegions * q) * (32 * kUnitBatches);
+  __device__ __forceinline__ int64_t unit_start(int64_t region, int64_t q) const {
+    return (region + (int64_t)kTickRegions * q) * (32 * (int64_t)ub);
   }
   __device__ __forceinline__ void fetch() {
     if ((threadIdx.x & 31) == 0) {
@@ -109,12 +110,17 @@ struct WarpBatches {
       pending = wr + atomicAdd(tick, 1);
     }
   }
-  __device__ __forceinline__ int64_t first(int* tick_) {
-    const int64_t w = warp();
-    tick = warps() >= kTickRegions ? tick_ + (w % kTickRegions) * kTickStride : nullptr;
+  // n: particles of the launch.  A unit holds up to kUnitBatches batches,
+  // fewer when there is too little work for every warp to get eight units
+  // (a 64^3 box has 9e3 batches for 7e3 warps).
+  __device__ __forceinline__ int64_t first(int* tick_, int64_t n) {
+    const int64_t w = warp(), nw = warps();
+    tick = nw >= kTickRegions ? tick_ + (w % kTickRegions) * kTickStride : nullptr;
     if (!tick) return 32 * w;
+    const int64_t per = n / (32 * 8 * nw);
+    ub = (int)(per < 1 ? 1 : per > kUnitBatches ? kUnitBatches : per);
     const int64_t b = unit_start(w % kTickRegions, w / kTickRegions);
-    unit_end = b + 32 * kUnitBatches;
+    unit_end = b + 32 * (int64_t)ub;
     fetch();
     return b;
   }
@@ -124,7 +130,7 @@ struct WarpBatches {
     if (base < unit_end) return base;
     const int q = __shfl_sync(0xffffffffu, pending, 0);
     const int64_t b = unit_start(warp() % kTickRegions, q);
-    unit_end = b + 32 * kUnitBatches;
+    unit_end = b + 32 * (int64_t)ub;
     fetch();
     return b;
   }

@@ -455,7 +455,7 @@ update_kernel(const float* __restrict__ X, int64_t n, BoxGeom bg, Grid3 g,
   // position is loaded one batch ahead
   const int lane = threadIdx.x & 31;
   WarpBatches wb;
-  int64_t base = wb.first(tick);
+  int64_t base = wb.first(tick, n);
   float nr[3] = {0.f, 0.f, 0.f};
   if (base + lane < n) {
     const int64_t p = base + lane;
@@ -543,7 +543,7 @@ bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, con
                  float4* __restrict__ gb4, float* __restrict__ Xb, int* tick) {
   const unsigned full = 0xffffffffu;
   WarpBatches wb;
-  for (int64_t base = wb.first(tick); base < n; base = wb.next(base)) {
+  for (int64_t base = wb.first(tick, n); base < n; base = wb.next(base)) {
     const bool live = base + (threadIdx.x & 31) < n;
     const int64_t p = live ? base + (threadIdx.x & 31) : n - 1;
     float v[3];
