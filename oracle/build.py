@@ -1,4 +1,4 @@
-"""ORACLE — test infrastructure only.  Builds the checkers.
+"""ORACLE — test infrastructure only.  Builds the oracle's C libraries.
 
 build(): liborc.so from cic_oracle.c.  gcc -O2 -ffp-contract=off keeps every
 product and sum separately rounded, as in the reference's x86-64 build (no

@@ -1,13 +1,14 @@
 /*
  * ORACLE — test infrastructure only.  CPU restatement of the reference's
  * single-rank cloud-in-cell loops, used by tests/, the smoke check and the
- * CPU-baseline leg of bench.py as the checker.  Nothing in the product links
- * or calls this file.
+ * CPU-baseline leg of bench.py to check results against.  Nothing in the
+ * product links or calls this file.
  *
- * Parity status: the reference itself cannot be built here (parops_fast.h
- * needs <mpi.h>, parfft.h needs FFTW3-MPI; neither is installed), so this
- * restatement is pinned by known-answer tests rather than by reference
- * output: parity unpinned against the reference binary.
+ * Parity status: pinned.  The reference's own CIC loops (lib/parops_fast.h)
+ * are compiled from its source with a world-size-one MPI stand-in
+ * (oracle/ref_stub/mpi.h, oracle/build.py: build_ref) and
+ * tests/test_ref_pin.py requires this restatement's outputs to equal theirs
+ * bit for bit.
  *
  * Restated functions (world size one: every particle is local, edges are
  * [0, N) on each axis, the decomposition keeps input order):

@@ -1,6 +1,6 @@
 """ORACLE — test infrastructure only.  FP64 restatement of the LDL pipeline
 and of its gradient, used by tests/, the smoke check and bench.py's CPU
-baseline as the checker.
+baseline to check results against.
 
 Forward (model.py): per layer (model.py:186-212 "sm", 137-179 "dm")
     rho   = paint(X, 1) * fact                    fact = prod(Nmesh) / Npart

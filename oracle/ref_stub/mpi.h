@@ -1,8 +1,8 @@
 /*
  * ORACLE — test infrastructure only.  A world-size-one stand-in for the few
  * MPI calls that the reference's CIC header makes, so that its loops can be
- * compiled from the reference's own source into oracle/_ref/ and used as the
- * checker.  Nothing in the product includes this file.
+ * compiled from the reference's own source into oracle/_ref/ and the
+ * oracle checked against them.  Nothing in the product includes this file.
  *
  * One process is the whole communicator: size 1, rank 0.  A datatype is its
  * size in bytes; MPI_Alltoall and MPI_Alltoallv copy the rank's own block
