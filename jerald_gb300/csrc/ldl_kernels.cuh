@@ -543,28 +543,56 @@ bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, con
                  float4* __restrict__ gb4, float* __restrict__ Xb, int* tick) {
   const unsigned full = 0xffffffffu;
   WarpBatches wb;
+  const int nax[3] = {g.nx, g.ny, g.nz};
+  // Warps whose 32 particles all lie inside the mesh (nearly all) skip the
+  // per-corner validity flags, separately for the two stencils.
+  auto inside = [&](const float q[3], bool live) {
+    bool in = live;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) in = in && (unsigned)(int)q[a] < (unsigned)nax[a];
+    return __all_sync(full, in);
+  };
+  auto corners = [&](const float q[3], bool fast, Corners<float>& c, float lo[3], float hi[3]) {
+    if (fast) cic_corners_inrange(q, g, c);
+    else cic_corners(q, g, c);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { hi[a] = c.d[a]; lo[a] = __fsub_rn(1.f, c.d[a]); }
+  };
   for (int64_t base = wb.first(tick, n); base < n; base = wb.next(base)) {
     const bool live = base + (threadIdx.x & 31) < n;
     const int64_t p = live ? base + (threadIdx.x & 31) : n - 1;
     float v[3];
     {
+      float q[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) q[a] = box_to_mesh_fast(__ldg(Xn + 3 * p + a), bg.box[a], bg.dw[a]);
+      const bool fast = inside(q, live);
       Corners<float> c;
       float lo[3], hi[3];
-      particle_setup(Xn, p, bg, g, c, lo, hi);
+      corners(q, fast, c, lo, hi);
       float r[8];
+      if (fast) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int bits = corner_axis_bits(k);
-        r[k] = corner_ok(c, bits) ? __ldg(rb + corner_offset(c, bits, g)) : 0.f;
+        for (int k = 0; k < 8; ++k) r[k] = __ldg(rb + corner_offset(c, corner_axis_bits(k), g));
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int bits = corner_axis_bits(k);
+          r[k] = corner_ok(c, bits) ? __ldg(rb + corner_offset(c, bits, g)) : 0.f;
+        }
       }
       float a[3];
       cic_grad(r, lo, hi, bg.dw, a);
 #pragma unroll
       for (int e = 0; e < 3; ++e) v[e] = live ? (Xbp ? __ldg(Xbp + 3 * p + e) + a[e] : a[e]) : 0.f;
     }
+    float q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) q[a] = box_to_mesh_fast(__ldg(X + 3 * p + a), bg.box[a], bg.dw[a]);
+    const bool fast = inside(q, live);
     Corners<float> c;
     float lo[3], hi[3];
-    particle_setup(X, p, bg, g, c, lo, hi);
+    corners(q, fast, c, lo, hi);
     float a[3] = {0.f, 0.f, 0.f};
     float4 s4[8];
     if (GATHER) {
@@ -573,14 +601,14 @@ bwd_fused_kernel(const float* __restrict__ Xn, const float* __restrict__ rb, con
       for (int k = 0; k < 8; ++k) {
         const int bits = corner_axis_bits(k);
         const float4 gv = __ldg(g4 + corner_offset(c, bits, g));
-        u[k] = corner_ok(c, bits) ? v[0] * gv.x + v[1] * gv.y + v[2] * gv.z : 0.f;
+        u[k] = (fast || corner_ok(c, bits)) ? v[0] * gv.x + v[1] * gv.y + v[2] * gv.z : 0.f;
       }
       cic_grad(u, lo, hi, bg.dw, a);
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int bits = corner_axis_bits(k);
-      const float w = corner_ok(c, bits) ? wprod(lo, hi, bits) : 0.f;
+      const float w = (fast || corner_ok(c, bits)) ? wprod(lo, hi, bits) : 0.f;
       s4[k] = make_float4(v[0] * w, v[1] * w, v[2] * w, 0.f);
     }
     const Pairing pr = zpair32_flags(live ? pair_key(c, g) : kNoPair);
