@@ -80,11 +80,13 @@ def test_fused_hi_matches_plain_f64(sparse, L1, mode):
     assert _rel(g, gp).max() < 1e-2, msg
 
 
-@pytest.mark.parametrize("variant", ["generic", "recompute_3", "mask_graph"])
+@pytest.mark.parametrize("variant", ["generic", "recompute_3", "mask_graph", "mesh_48"])
 def test_fused_hi_variants(variant):
     """The generic (non-pipelined) passes, three layers with the recompute
-    memory plan, and a training mask through a captured CUDA graph."""
-    n, box = 32, 100.0
+    memory plan, a training mask through a captured CUDA graph, and a 48^3
+    mesh (x and y passes on the 3 x 2^k pipelined schedules, the star map's
+    own x pass included)."""
+    n, box = (48, 150.0) if variant == "mesh_48" else (32, 100.0)
     nstep = 3 if variant == "recompute_3" else 2
     X, p, sm, tgt = _inputs(n, box, True, 90, nstep=nstep)
     mask = (np.random.default_rng(91).integers(0, 2, (n,) * 3).astype(np.float32)
