@@ -365,11 +365,22 @@ readout_kernel(PosSrc<T> src, int64_t n, const T* __restrict__ field, Grid3 g,
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       T acc = T(0);
+      // a particle inside the mesh has every corner valid: the products
+      // with the validity flag are the identity (bit for bit) and are left
+      // out; others keep the reference's out-of-range semantics
+      if (c[i].ok[0][0] && c[i].ok[1][0] && c[i].ok[2][0]) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int bits = corner_axis_bits(k);
-        T t = mul_rn(mul_rn(corner_weight(lo[i], hi[i], bits), v[i][k]), corner_ok(c[i], bits) ? T(1) : T(0));
-        acc = (k == 0) ? t : add_rn(acc, t);
+        for (int k = 0; k < 8; ++k) {
+          const T t = mul_rn(corner_weight(lo[i], hi[i], corner_axis_bits(k)), v[i][k]);
+          acc = (k == 0) ? t : add_rn(acc, t);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int bits = corner_axis_bits(k);
+          T t = mul_rn(mul_rn(corner_weight(lo[i], hi[i], bits), v[i][k]), corner_ok(c[i], bits) ? T(1) : T(0));
+          acc = (k == 0) ? t : add_rn(acc, t);
+        }
       }
       if (i == 0 || p0 + S < n) out[pp[i]] = acc;
     }
