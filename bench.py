@@ -766,7 +766,7 @@ def main():
     cpu = None
     if not args.no_cpu and rank == 0:
         try:
-            cpu = cpu_baseline_sample(min(128, n), n, steps=1)
+            cpu = cpu_baseline_sample(min(256, n), n, steps=3)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 

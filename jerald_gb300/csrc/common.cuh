@@ -177,9 +177,12 @@ __device__ __forceinline__ T box_to_mesh(T x, T box, T cell) {
 }
 
 // The same prelude with r * (N/L) instead of r / (L/N): one rounding more
-// (q within an ulp or two of box_to_mesh's), no division.  For kernels whose
+// (q within one ulp of box_to_mesh's), no division.  For kernels whose
 // results are compared within a tolerance (the fused step): the CIC weights
 // are continuous in q, so painted and gathered values move by a few ulps.
+// The cell (floor q) is box_to_mesh's for every float r when L/N = 25/16;
+// with other cell sizes it can be one lower or higher for r on a cell
+// boundary, where the weight moved across is an ulp of q.
 __device__ __forceinline__ float box_to_mesh_fast(float x, float box, float inv_cell) {
   float r;
   if (x >= 0.f && x < box) {
