@@ -125,3 +125,32 @@ def test_argument_errors_before_any_launch(libjld):
         libjld.jld_ldl_workspace_opt_f32(32, 32, 32, 1000, 2, 0)
     assert extra == 3 * 8 * 32 * 32 * 17 + 2 * 4 * 32 ** 3
     assert hi(None, f, 8, 4, 4, 4, fbox, 2, 1, 0, 0, f, f, None, f, f, 16, f) == 3
+
+
+def _c_examples():
+    txt = (ROOT / "INTEGRATION.md").read_text()
+    return re.findall(r"```c\n(.*?)```", txt, flags=re.S)
+
+
+def test_integration_c_examples_compile_and_link(libjld, tmp_path):
+    """The C examples of INTEGRATION.md build against include/jld.h with
+    -Wall -Werror and link against libjld and cudart with no undefined
+    symbol (compiled only, never run)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    nvcc = shutil.which("nvcc")
+    cuda = Path(nvcc).resolve().parents[1] if nvcc else Path("/usr/local/cuda")
+    if not gcc or not (cuda / "include" / "cuda_runtime.h").exists():
+        pytest.skip("gcc or the CUDA runtime headers are absent")
+    blocks = _c_examples()
+    assert len(blocks) >= 2
+    lib = Path(libjld._name).parent
+    for i, src in enumerate(blocks):
+        c = tmp_path / f"example{i}.c"
+        c.write_text(src)
+        cmd = [gcc, "-std=c11", "-Wall", "-Werror", "-shared", "-fPIC", "-I", str(ROOT / "include"),
+               "-I", str(cuda / "include"), str(c), "-o", str(tmp_path / f"example{i}.so"),
+               "-L", str(lib), "-ljld", "-L", str(cuda / "lib64"), "-lcudart", "-Wl,--no-undefined"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, f"example {i}:\n{r.stderr}"
