@@ -5,7 +5,7 @@ FFTW, its bindings JAX), so these fixtures hold the oracle's outputs for
 fixed seeded inputs; tests/test_golden.py pins the oracle to them on the CPU
 and tests/test_golden_gpu.py holds the CUDA path to them.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture ...]
 """
 from __future__ import annotations
 
@@ -90,11 +90,48 @@ def make_losstest():
                         loss=loss, lossv=lossv, grad=grad)
 
 
+def hi_fd_grad(n, box, p, X, tgt, sm):
+    """Central differences of the oracle's HI loss (L2), step 1e-4 max(|p|, 1)."""
+    from oracle.ldl import model_loss
+    g = np.empty(len(p))
+    for i in range(len(p)):
+        h = 1e-4 * max(abs(p[i]), 1.0)
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        lp = model_loss((n,) * 3, box, "HI", pp, X, tgt, 2, starmap=sm, L1=False)[0]
+        lm = model_loss((n,) * 3, box, "HI", pm, X, tgt, 2, starmap=sm, L1=False)[0]
+        g[i] = (lp - lm) / (2 * h)
+    return g
+
+
+def make_ldl_hi():
+    # the HI kind (model.py:213-247, 313-336): a sparse star map, a uniform target
+    from jerald_gb300 import synth
+    from oracle.ldl import model_loss
+    n, box = 16, 100.0
+    X = synth.zeldovich(n, box, 0.5, seed=5, dtype=np.float32).astype(np.float64)
+    sm = synth.star_map(n, box, 6).astype(np.float64)
+    tgt = np.random.default_rng(7).uniform(0.5, 1.5, (n, n, n))
+    p = np.asarray(synth.default_params_hi(2), dtype=np.float64)
+    loss_l1 = model_loss((n,) * 3, box, "HI", p, X, tgt, 2, starmap=sm, L1=True)[0]
+    loss_l2 = model_loss((n,) * 3, box, "HI", p, X, tgt, 2, starmap=sm, L1=False)[0]
+    np.savez_compressed(HERE / "ldl_hi16.npz", X=X, params=p, starmap=sm, target=tgt, box=box, n=n,
+                        loss_l1=loss_l1, loss_l2=loss_l2, grad_l2_fd=hi_fd_grad(n, box, p, X, tgt, sm))
+
+
+MAKERS = {
+    "cic_f32": lambda: make_cic(np.float32, "cic_f32.npz"),
+    "cic_f64": lambda: make_cic(np.float64, "cic_f64.npz"),
+    "fft": make_fft,
+    "ldl_sm16": make_ldl,
+    "losstest20": make_losstest,
+    "ldl_hi16": make_ldl_hi,
+}
+
 if __name__ == "__main__":
-    make_cic(np.float32, "cic_f32.npz")
-    make_cic(np.float64, "cic_f64.npz")
-    make_fft()
-    make_ldl()
-    make_losstest()
+    # python tests/golden/make_golden.py [fixture ...]   (default: all)
+    for name in sys.argv[1:] or MAKERS:
+        MAKERS[name]()
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -40,6 +40,32 @@ def test_ldl_fixture():
     assert abs(loss - float(f["loss"])) <= 1e-12 * abs(loss)
     np.testing.assert_allclose(g, f["grad_reference"], rtol=1e-9, atol=1e-20)
     np.testing.assert_allclose(o.backward("true"), f["grad_true"], rtol=1e-9, atol=1e-20)
+    od = LDLOracle((n,) * 3, float(f["box"]), kind="dm", L1=False)
+    loss_dm, g_dm = od.loss_and_grad(f["params"][:10], f["X"], np.ones((n,) * 3), 2, mode="true")
+    assert abs(loss_dm - float(f["loss_dm"])) <= 1e-12 * abs(loss_dm)
+    np.testing.assert_allclose(g_dm, f["grad_dm_true"], rtol=1e-9, atol=1e-20)
+
+
+def test_ldl_hi_fixture():
+    """The HI kind's FP64 forward (model.py:213-247, 313-336) and the central
+    differences of its L2 loss; the differences agree with those at half the
+    step to 4e-7 per component, so they pin the layer gradients (1e-7 of the
+    final map's at these parameters) as well as the map's."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", G / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    from oracle.ldl import model_loss
+    f = np.load(G / "ldl_hi16.npz")
+    n, box = int(f["n"]), float(f["box"])
+    args = (f["params"], f["X"], f["target"], 2)
+    assert f["params"].shape == (32,)
+    for L1, key in ((True, "loss_l1"), (False, "loss_l2")):
+        loss = model_loss((n,) * 3, box, "HI", *args, starmap=f["starmap"], L1=L1)[0]
+        assert abs(loss - float(f[key])) <= 1e-12 * abs(loss)
+    g = mg.hi_fd_grad(n, box, f["params"], f["X"], f["target"], f["starmap"])
+    # atol: a rounding change of the forward moves a difference by ~1e-12
+    np.testing.assert_allclose(g, f["grad_l2_fd"], rtol=1e-7, atol=1e-10)
 
 
 def test_losstest_fixture():
