@@ -10,6 +10,7 @@
 #include "bins.cuh"
 #include "ldl_kernels.cuh"
 #include "ldl_pipe.cuh"
+#include "nvtx.cuh"
 #include "hi_kernels.cuh"
 #include "pipe_host.cuh"
 #include "zpipe.cuh"
@@ -162,6 +163,7 @@ static void launch_finish(cudaStream_t st, const double* part, int nblocks, int 
 }
 
 static int ldl_step(const StepArgs& a) {
+  const ScopedRange step_range("jld_ldl_step");
   const int nx = a.nx, ny = a.ny, nz = a.nz, h = nz / 2;
   const bool hi = a.kind == 2;
   const LdlLayout L = ldl_layout(nx, ny, nz, a.N, a.nstep, a.options, hi);
@@ -536,6 +538,7 @@ static int ldl_step(const StepArgs& a) {
   // ---------------- forward layers (density of layer l+1 painted after its update)
   if ((s = paint_into(Xl(0), rho))) return s;
   for (int l = 0; l < a.nstep; ++l) {
+    const ScopedRange layer_range("jld forward layer %d", l);
     float4* g4_l = g4_of(l);
     if (hi && (s = star_spectrum(l, (float2*)(ws + L.off_s2) + (size_t)L.H * l))) return s;
     if ((s = force_mesh(l, g4_l))) return s;
@@ -548,6 +551,7 @@ static int ldl_step(const StepArgs& a) {
   // ---------------- final map, loss and its cotangent
   float* rho_f = rho + (size_t)L.C * a.nstep;
   {
+    const ScopedRange map_range("jld final map and loss");
     const LossFields lf{rho_f, a.target, a.mask, a.field2, a.maskvalid};
     const float* fprm = a.params + npot * a.nstep;
     const int nparam = npot * a.nstep + (a.kind == 0 ? 3 : (a.kind == 2 ? kHiFinalParams : 0));
@@ -631,6 +635,7 @@ static int ldl_step(const StepArgs& a) {
 
   // ---------------- adjoint layers
   for (int l = a.nstep - 1; l >= 0; --l) {
+    const ScopedRange layer_range("jld adjoint layer %d", l);
     const float* prm = a.params + npot * l;
     float* rho_l = rho + (size_t)L.C * l;
     float2* S_l = Sbuf + (size_t)L.H * l;
