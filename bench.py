@@ -146,11 +146,13 @@ def make_target(pos, n, box, params, device, nstep: int = 2):
 
 def workload_config(n: int, nparts: int, box: float, nstep: int, recompute: bool = False, world: int = 1):
     """The `config` object of both arms' lines."""
+    inputs = 12 * int(nparts) + 4 * n ** 3  # positions and target
     return {"workload": f"clustered {n}^3 particles +10% halos on a {n}^3 mesh, {nstep} sm layers + "
                         f"ReLU map, L1 loss, fwd+adjoint ({5 * nstep + 3} grads)",
             "nmesh": n, "nparts": int(nparts), "box": box, "nstep": nstep, "kind": "sm",
             "memory_plan": "recompute force meshes" if recompute else "checkpoint",
-            "l2": "inputs larger than L2 (no flush)",
+            "l2": ("inputs larger than L2 (no flush)" if inputs > 129e6
+                   else "inputs fit in L2 (no flush: a small configuration)"),
             "parallelism": f"{world} replicas" if world > 1 else "single GPU"}
 
 
@@ -280,6 +282,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    world = int(os.environ.get("WORLD_SIZE", "1"))  # for the shared `config` only
     from jerald_gb300 import synth
     from oracle import cic as ocic
     from oracle import fft as offt
@@ -310,7 +313,8 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * dt, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice + Gaussian halos)",
-            "impl": "reference", "config": workload_config(n, len(X), box, nstep), "cpu_baseline": cb,
+            "impl": "reference", "config": workload_config(n, len(X), box, nstep, args.recompute, world),
+            "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "loss": loss}
     print(json.dumps(line), flush=True)
